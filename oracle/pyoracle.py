@@ -1,0 +1,207 @@
+"""ctypes wrapper of the C oracle ``mstoracle.c`` (test infrastructure only).
+
+Arrays come back as numpy copies; the C mesh is freed when the Python object
+is collected.  Layouts follow ``mstoracle.h``: states ``[n_cells, 4]``, face
+flux matrices ``[n_faces, 2, 4]``, gradients ``[n_cells, 2, 4]``.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+AUSM, ROE = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_uint8)
+
+
+class _OMesh(C.Structure):
+    _fields_ = [
+        ("n_nodes", C.c_int), ("n_cells", C.c_int), ("n_faces", C.c_int),
+        ("n_int_faces", C.c_int), ("n_zones", C.c_int),
+        ("n_inner", C.c_int), ("n_bond1", C.c_int), ("n_bond2", C.c_int),
+        ("zone", _ip), ("node_xy", _dp), ("face_nodes", _ip),
+        ("face_cells", _ip), ("face_type", _ip), ("face_ctr", _dp),
+        ("face_dir", _dp), ("face_area", _dp), ("face_eta0", _dp),
+        ("face_dac", _ip), ("face_flag", _up), ("cell_ptr", _ip),
+        ("cell_faces", _ip), ("cell_nb", _ip), ("cell_dof", _dp),
+        ("cell_eta0c", _dp), ("cell_ctr", _dp), ("cell_vol", _dp),
+        ("inner", _ip), ("bond1", _ip), ("bond2", _ip),
+    ]
+
+
+class _OParams(C.Structure):
+    _fields_ = [("flux", C.c_int), ("order", C.c_int),
+                ("inlet_q", C.c_double * 4)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        L.om_mesh_read.argtypes = [C.c_char_p, C.POINTER(C.POINTER(_OMesh))]
+        L.om_mesh_from_arrays.argtypes = [
+            C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, C.c_int, _ip,
+            C.POINTER(C.POINTER(_OMesh))]
+        L.om_mesh_free.argtypes = [C.POINTER(_OMesh)]
+        L.om_default_params.argtypes = [C.POINTER(_OParams)]
+        L.om_reference_inlet.argtypes = [_dp]
+        for fn in ("om_ausm_flux", "om_roe_flux"):
+            getattr(L, fn).argtypes = [_dp, _dp, C.c_int, _dp]
+        L.om_gradient.argtypes = [C.POINTER(_OMesh), _dp, _dp, _dp]
+        L.om_face_flux.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParams),
+                                   _dp, _dp, _dp]
+        L.om_gather.argtypes = [C.POINTER(_OMesh), _dp, _dp]
+        L.om_solve.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParams), _dp,
+                               C.c_double, _dp, _dp]
+        L.om_linf_change.argtypes = [C.c_int, _dp, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Mesh:
+    """Oracle mesh: the reference's MshBlock flattened to arrays."""
+
+    def __init__(self, ptr):
+        self._p = ptr
+        m = ptr.contents
+        self.n_nodes, self.n_cells = m.n_nodes, m.n_cells
+        self.n_faces, self.n_int_faces = m.n_faces, m.n_int_faces
+        nN, nC, nF, nZ = m.n_nodes, m.n_cells, m.n_faces, m.n_zones
+
+        def arr(p, n, shape=None):
+            a = np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0)
+            return a.reshape(shape) if shape else a
+
+        self.zone = arr(m.zone, 4 * nZ, (nZ, 4))
+        self.node_xy = arr(m.node_xy, 2 * nN, (nN, 2))
+        self.face_nodes = arr(m.face_nodes, 2 * nF, (nF, 2))
+        self.face_cells = arr(m.face_cells, 2 * nF, (nF, 2))
+        self.face_type = arr(m.face_type, nF)
+        self.face_ctr = arr(m.face_ctr, 2 * nF, (nF, 2))
+        self.face_dir = arr(m.face_dir, 2 * nF, (nF, 2))
+        self.face_area = arr(m.face_area, nF)
+        self.face_eta0 = arr(m.face_eta0, nF)
+        self.face_dac = arr(m.face_dac, nF)
+        self.face_flag = arr(m.face_flag, 2 * nF, (nF, 2))
+        self.cell_ptr = arr(m.cell_ptr, nC + 1)
+        tot = int(self.cell_ptr[-1])
+        self.cell_faces = arr(m.cell_faces, tot)
+        self.cell_nb = arr(m.cell_nb, tot)
+        self.cell_dof = arr(m.cell_dof, 2 * tot, (tot, 2))
+        self.cell_eta0c = arr(m.cell_eta0c, tot)
+        self.cell_ctr = arr(m.cell_ctr, 2 * nC, (nC, 2))
+        self.cell_vol = arr(m.cell_vol, nC)
+        self.inner = arr(m.inner, m.n_inner)
+        self.bond1 = arr(m.bond1, m.n_bond1)
+        self.bond2 = arr(m.bond2, m.n_bond2)
+
+    def __del__(self):
+        try:
+            lib().om_mesh_free(self._p)
+        except Exception:
+            pass
+
+
+def read_msh(path):
+    p = C.POINTER(_OMesh)()
+    rc = lib().om_mesh_read(os.fsencode(path), C.byref(p))
+    if rc != 0:
+        raise ValueError(f"oracle: cannot read mesh {path} (status {rc})")
+    return Mesh(p)
+
+
+def mesh_from_arrays(node_xy, face_nodes, face_cells, zones, n_cells):
+    node_xy = _f64(node_xy)
+    fn = np.ascontiguousarray(face_nodes, dtype=np.int32)
+    fc = np.ascontiguousarray(face_cells, dtype=np.int32)
+    z = np.ascontiguousarray(zones, dtype=np.int32)
+    p = C.POINTER(_OMesh)()
+    rc = lib().om_mesh_from_arrays(len(node_xy), _d(node_xy), int(n_cells),
+                                   len(fn), _i(fn), _i(fc), len(z), _i(z),
+                                   C.byref(p))
+    if rc != 0:
+        raise ValueError(f"oracle: bad mesh arrays (status {rc})")
+    return Mesh(p)
+
+
+def params(flux=AUSM, order=1, inlet_q=None):
+    p = _OParams()
+    lib().om_default_params(C.byref(p))
+    p.flux, p.order = flux, order
+    if inlet_q is not None:
+        for k in range(4):
+            p.inlet_q[k] = float(inlet_q[k])
+    return p
+
+
+def reference_inlet():
+    q = np.zeros(4)
+    lib().om_reference_inlet(_d(q))
+    return q
+
+
+def riemann(flux, ql, qr, d):
+    ql, qr = _f64(ql), _f64(qr)
+    f = np.zeros(4)
+    fn = lib().om_roe_flux if flux == ROE else lib().om_ausm_flux
+    fn(_d(ql), _d(qr), int(d), _d(f))
+    return f
+
+
+def gradient(mesh, q):
+    q = _f64(q)
+    faceq = np.zeros((mesh.n_faces, 4))
+    grad = np.zeros((mesh.n_cells, 2, 4))
+    lib().om_gradient(mesh._p, _d(q), _d(faceq), _d(grad))
+    return faceq, grad
+
+
+def face_flux(mesh, prm, q, grad=None):
+    q = _f64(q)
+    F = np.zeros((mesh.n_faces, 2, 4))
+    g = _d(_f64(grad)) if grad is not None else _dp()
+    lib().om_face_flux(mesh._p, C.byref(prm), _d(q), g, _d(F))
+    return F
+
+
+def gather(mesh, F):
+    F = _f64(F)
+    R = np.zeros((mesh.n_cells, 4))
+    lib().om_gather(mesh._p, _d(F), _d(R))
+    return R
+
+
+def solve(mesh, prm, q, dt):
+    """One RhoSolver::solve(): returns (qnew, R)."""
+    q = _f64(q)
+    qn = np.zeros_like(q)
+    R = np.zeros_like(q)
+    lib().om_solve(mesh._p, C.byref(prm), _d(q), float(dt), _d(qn), _d(R))
+    return qn, R
+
+
+def linf_change(qold, qnew):
+    qold, qnew = _f64(qold), _f64(qnew)
+    r = np.zeros(4)
+    lib().om_linf_change(len(qold), _d(qold), _d(qnew), _d(r))
+    return r

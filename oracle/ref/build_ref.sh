@@ -1,0 +1,98 @@
+#!/usr/bin/env bash
+# Builds the reference oracle (test infrastructure only) into oracle/_ref.
+#
+# The reference's density-based path is compiled from its own sources where
+# they lie (MSTCFD_REF_SRC, default the read-only reference checkout); nothing
+# is copied.  Per variant, oracle/_ref/<variant>/src is a mirror of the
+# reference tree made of symlinks, plus
+#   * case-fixing symlinks for the includes the sources spell differently
+#     from the file names (sparseSolverNUM.h, sparseSolver.h/.cpp, solverRoe.h),
+#   * include/CONST.h = the reference CONST.h (linked as CONST_ref.h) followed
+#     by the variant's overrides (RHO_P 0, ACCURACY, RHOSOLVER, threads),
+#   * an empty pSolver/PSolver.h (the pressure solvers are not on this path and
+#     need Eigen/Sparse plus a header the reference does not ship),
+# and Eigen comes from the project's shim in oracle/ref/eigen_shim.
+# -ffp-contract=off keeps gcc from fusing multiply-adds (aarch64 fuses by
+# default), so the oracle rounds every operation like the parity kernels do.
+set -euo pipefail
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT=${MSTCFD_REF_OUT:-$HERE/../_ref}
+REF=${MSTCFD_REF_SRC:-/root/reference/MST-CFD}
+THREADS=${MSTCFD_REF_THREADS:-$(nproc)}
+CXX=${CXX:-g++}
+CXXFLAGS="-std=c++20 -O2 -fopenmp -ffp-contract=off -w -I$HERE/eigen_shim"
+
+if [ ! -f "$REF/rhoSolver/RhoSolver.cpp" ]; then
+  echo "build_ref: reference sources not found at $REF" >&2
+  exit 3
+fi
+mkdir -p "$OUT"
+OUT=$(cd "$OUT" && pwd)
+
+mirror() {  # variant-dir accuracy flux-class
+  local V=$1 ACC=$2 FLUX=$3
+  local S="$OUT/$V/src"
+  rm -rf "$OUT/$V"
+  mkdir -p "$S"
+  for d in include mesh work data rhoSolver time lusolver pSolver; do
+    mkdir -p "$S/$d"
+  done
+  for d in mesh work data rhoSolver time lusolver; do
+    for f in "$REF/$d"/*; do ln -s "$f" "$S/$d/$(basename "$f")"; done
+  done
+  ln -s "$REF/lusolver/SparseSolverNUM.h" "$S/lusolver/sparseSolverNUM.h"
+  ln -s "$REF/lusolver/SparseSolver.h" "$S/lusolver/sparseSolver.h"
+  ln -s "$REF/lusolver/SparseSolver.cpp" "$S/lusolver/sparseSolver.cpp"
+  ln -s "$REF/rhoSolver/SolverRoe.h" "$S/rhoSolver/solverRoe.h"
+  ln -s "$REF/include/CONST.h" "$S/include/CONST_ref.h"
+  printf '#pragma once\n' > "$S/pSolver/PSolver.h"
+  cat > "$S/include/CONST.h" <<EOF
+#pragma once
+#include "CONST_ref.h"
+#undef RHO_P
+#define RHO_P 0
+#undef ACCURACY
+#define ACCURACY $ACC
+#undef RHOSOLVER
+#define RHOSOLVER $FLUX
+#undef NUM_CPU_THREADS
+#define NUM_CPU_THREADS $THREADS
+EOF
+}
+
+SRCS="mesh/Cell.cpp mesh/Face.cpp mesh/Node.cpp mesh/FacesInf.cpp mesh/MshBlock.cpp
+      work/FUNCTION.cpp data/AllData.cpp rhoSolver/RhoSolver.cpp
+      rhoSolver/SolverRoe.cpp rhoSolver/SolverAusm.cpp time/Time.cpp"
+
+build_variant() {  # variant-dir accuracy flux-class
+  local V=$1
+  mirror "$@"
+  local S="$OUT/$V/src" O="$OUT/$V/obj"
+  mkdir -p "$O"
+  local objs=""
+  for f in $SRCS; do
+    local o="$O/$(echo "$f" | tr '/' '_').o"
+    objs="$objs $o"
+    $CXX $CXXFLAGS -I"$S" -c "$S/$f" -o "$o" &
+  done
+  $CXX $CXXFLAGS -I"$S" -c "$HERE/harness_rho.cpp" -o "$O/harness_rho.o" &
+  wait
+  $CXX $CXXFLAGS $objs "$O/harness_rho.o" -o "$OUT/ref_rho_$V"
+}
+
+build_variant ausm_o1 1 SolverAusm &
+build_variant ausm_o2 2 SolverAusm &
+build_variant roe_o1 1 solverRoe &
+build_variant roe_o2 2 solverRoe &
+wait
+
+# lusolver: the scalar SparseSolverNUM and the block SparseSolver template.
+S="$OUT/ausm_o1/src"
+$CXX $CXXFLAGS -I"$S" "$S/lusolver/SparseSolverNUM.cpp" "$S/work/FUNCTION.cpp" \
+  "$HERE/harness_lu.cpp" -o "$OUT/ref_lu"
+
+for v in ausm_o1 ausm_o2 roe_o1 roe_o2; do
+  test -x "$OUT/ref_rho_$v"
+done
+test -x "$OUT/ref_lu"
+echo "build_ref: ok ($OUT)"

@@ -1,0 +1,114 @@
+"""Runs the reference compiled into oracle/_ref (test infrastructure only).
+
+Only usable where the reference checkout exists (``build.ref_available()``);
+tests that need it skip elsewhere and rely on the committed golden fixtures.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from . import build as _build
+
+VARIANTS = ("ausm_o1", "ausm_o2", "roe_o1", "roe_o2")
+
+
+def variant(flux, order):
+    return f"{'roe' if flux == 1 else 'ausm'}_o{order}"
+
+
+class RefRun:
+    """Outputs of one reference harness run (see oracle/ref/harness_rho.cpp)."""
+
+    def __init__(self, outdir):
+        self.dir = outdir
+
+    def _load(self, name, dtype, shape=None):
+        a = np.fromfile(os.path.join(self.dir, name), dtype=dtype)
+        return a.reshape(shape) if shape else a
+
+    def __getattr__(self, key):
+        spec = {
+            "counts": ("counts.i32", np.int32, None),
+            "zones": ("zones.i32", np.int32, (-1, 4)),
+            "nodes": ("nodes.f64", np.float64, (-1, 2)),
+            "face_nodes": ("face_nodes.i32", np.int32, (-1, 2)),
+            "face_cells": ("face_cells.i32", np.int32, (-1, 2)),
+            "face_dac": ("face_dac.i32", np.int32, None),
+            "face_type": ("face_type.i32", np.int32, None),
+            "face_center": ("face_center.f64", np.float64, (-1, 2)),
+            "face_direct": ("face_direct.f64", np.float64, (-1, 2)),
+            "face_area": ("face_area.f64", np.float64, None),
+            "face_eta0": ("face_eta0.f64", np.float64, None),
+            "face_flag": ("face_flag.u8", np.uint8, (-1, 2)),
+            "cell_ptr": ("cell_ptr.i32", np.int32, None),
+            "cell_faces": ("cell_faces.i32", np.int32, None),
+            "cell_nbcells": ("cell_nbcells.i32", np.int32, None),
+            "cell_dof": ("cell_dof.f64", np.float64, (-1, 2)),
+            "cell_eta0c": ("cell_eta0c.f64", np.float64, None),
+            "cell_center": ("cell_center.f64", np.float64, (-1, 2)),
+            "cell_volume": ("cell_volume.f64", np.float64, None),
+            "bond_counts": ("bond_counts.i32", np.int32, None),
+            "inner": ("inner.i32", np.int32, None),
+            "bond1": ("bond1.i32", np.int32, None),
+            "bond2": ("bond2.i32", np.int32, None),
+            "q0": ("q0.f64", np.float64, (-1, 4)),
+            "flux": ("flux.f64", np.float64, (-1, 2, 4)),
+            "resid": ("resid.f64", np.float64, (-1, 4)),
+            "qnew": ("qnew.f64", np.float64, (-1, 4)),
+            "faceq": ("faceq.f64", np.float64, (-1, 4)),
+            "q_steps": ("q_steps.f64", np.float64, (-1, 4)),
+        }
+        if key not in spec:
+            raise AttributeError(key)
+        return self._load(*spec[key])
+
+    def time_log(self):
+        """L-infinity residual rows the reference's Time loop logged."""
+        rows = []
+        with open(os.path.join(self.dir, "time.log")) as f:
+            for line in f:
+                if line.strip():
+                    rows.append([float(x) for x in line.split()])
+        return np.array(rows)
+
+
+def run(mesh_path, flux=0, order=1, q0=None, dt=None, remap5=False,
+        time_steps=0, outdir=None):
+    """Run ref_rho_<variant> once; returns RefRun."""
+    if not _build.build_ref():
+        raise RuntimeError("reference sources not available")
+    exe = os.path.join(_build.REF_OUT, "ref_rho_" + variant(flux, order))
+    outdir = outdir or tempfile.mkdtemp(prefix="mstref_")
+    args = [exe, os.path.abspath(mesh_path), outdir]
+    if q0 is not None:
+        qp = os.path.join(outdir, "q0_in.f64")
+        np.ascontiguousarray(q0, dtype=np.float64).tofile(qp)
+        args += ["--q0", qp]
+    if dt is not None:
+        args += ["--dt", repr(float(dt))]
+    if remap5:
+        args += ["--remap5to3"]
+    if time_steps:
+        args += ["--time-steps", str(int(time_steps))]
+    subprocess.run(args, check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    return RefRun(outdir)
+
+
+def run_lu(mode, dim, rows, cols, ops, vals, b, x0):
+    """Run the reference lusolver harness (mode 0 ILU-SGS, 1 GS, 2 block)."""
+    if not _build.build_ref():
+        raise RuntimeError("reference sources not available")
+    d = tempfile.mkdtemp(prefix="mstlu_")
+    inp, out = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+    with open(inp, "wb") as f:
+        np.array([mode, dim, len(rows)], np.int32).tofile(f)
+        for a in (rows, cols, ops):
+            np.ascontiguousarray(a, dtype=np.int32).tofile(f)
+        for a in (vals, b, x0):
+            np.ascontiguousarray(a, dtype=np.float64).tofile(f)
+    subprocess.run([os.path.join(_build.REF_OUT, "ref_lu"), inp, out],
+                   check=True, stdout=subprocess.DEVNULL)
+    return np.fromfile(out, dtype=np.float64)
