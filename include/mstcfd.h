@@ -1,0 +1,208 @@
+/* mstcfd.h -- C ABI of the GB300 (sm_103a) density-based unstructured
+ * finite-volume residual path.
+ *
+ * Drop-in boundary for MST-CFD's RhoSolver (rhoSolver/RhoSolver.h:14-56 in
+ * the reference).  Every entry point returns an mst_status, never aborts and
+ * never lets an exception cross the boundary.  Plain pointers and sizes
+ * only.  The caller owns host buffers; a context owns its device buffers and
+ * one CUDA stream.  One context per host thread; contexts are independent.
+ *
+ * Numbering: cells and faces keep the numbering of the .msh file (0-based);
+ * any device-side renumbering is internal and invisible at this boundary.
+ * States are AoS rows of 4 doubles (rho, rho*u, rho*v, E) with a caller
+ * stride (in doubles, >= 4), so an array of the reference's VCTDIMU
+ * (Eigen Matrix<double,4,1>, 32-byte stride) is passed as-is with stride 4.
+ */
+#ifndef MSTCFD_H
+#define MSTCFD_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSTCFD_ABI_VERSION 1
+
+typedef enum mst_status {
+  MST_OK = 0,
+  MST_EINVAL = 1,      /* bad argument */
+  MST_EMESH = 2,       /* malformed or unsupported mesh */
+  MST_ECUDA = 3,       /* CUDA runtime error (see mst_last_error) */
+  MST_EDIVERGED = 4,   /* NaN or non-positive density/pressure */
+  MST_ETIMEOUT = 5,    /* a bounded device wait gave up */
+  MST_ENOMEM = 6,      /* host or device allocation failed */
+  MST_EUNSUPPORTED = 7 /* option combination not built */
+} mst_status;
+
+/* Riemann flux (reference: CONST.h:10 RHOSOLVER) */
+enum { MST_FLUX_AUSM = 0, MST_FLUX_ROE = 1 };
+/* TVD limiter for 2nd order (none = the reference's unlimited scheme) */
+enum {
+  MST_LIMITER_NONE = 0,
+  MST_LIMITER_MINMOD = 1,
+  MST_LIMITER_VANLEER = 2,
+  MST_LIMITER_VANALBADA = 3
+};
+/* Arithmetic of reconstruction + flux.  FP64_EXACT rounds every operation
+ * like the reference (no fused multiply-add); FP64 allows FMA; FP32 runs
+ * reconstruction and flux in float and keeps the state, the residual
+ * accumulation and the norms in double. */
+enum { MST_PREC_FP64_EXACT = 0, MST_PREC_FP64 = 1, MST_PREC_FP32 = 2 };
+/* Time integration: one forward-Euler stage (RhoSolver.cpp:64) or the
+ * two-stage SSP Runge-Kutta (Heun) scheme. */
+enum { MST_TIME_EULER = 0, MST_TIME_RK2 = 1 };
+/* Time step: fixed (RhoSolver::setDT), global CFL, or local (per-cell) CFL */
+enum { MST_DT_FIXED = 0, MST_DT_CFL_GLOBAL = 1, MST_DT_CFL_LOCAL = 2 };
+
+typedef struct mst_params {
+  int flux;          /* MST_FLUX_* */
+  int order;         /* 1 or 2 (reference: CONST.h:6 ACCURACY) */
+  int limiter;       /* MST_LIMITER_* (order 2 only) */
+  int precision;     /* MST_PREC_* */
+  int time_scheme;   /* MST_TIME_* */
+  int dt_mode;       /* MST_DT_* */
+  double dt;         /* fixed step; reference default 1/STEP_TIME = 1/4000 */
+  double cfl;        /* CFL number for the CFL modes */
+  double inlet_q[4]; /* type-10 boundary state (reference: CONST.h:77-83) */
+  /* 1 = reproduce the reference bit-for-bit, including its quirks (left/right
+   * flags as MshBlock.cpp:281-305 sets them, boundary face values from
+   * nInt-1, symmetry ghost of RhoSolver.cpp:320-350).  0 = corrected
+   * behaviour (geometric left/right, boundary loops from nInt, 2nd-order
+   * symmetry = mirrored reconstructed state, 2nd-order outlet =
+   * reconstructed zero-gradient). */
+  int reference_quirks;
+  int reserved[7];
+} mst_params;
+
+/* Reference defaults: AUSM+, 1st order, FP64_EXACT, Euler, DT = 1/4000,
+ * inlet state of CONST.h, quirks on. */
+void mst_params_default(mst_params *p);
+
+/* ------------------------------------------------------------------ */
+/* meshes                                                              */
+/* ------------------------------------------------------------------ */
+typedef struct mst_mesh mst_mesh;
+
+/* Reads a Fluent ASCII 2D mesh (the subset of MshBlock::readMsh,
+ * mesh/MshBlock.cpp:5-18, :75-432) and builds its geometry exactly as the
+ * reference does (Face::setCenter Face.cpp:8-19, Cell::setCenter/setVolume
+ * Cell.cpp:6-50, orientation flags MshBlock.cpp:281-305, directOfNbFaces
+ * :307-318, eta0 :319-334).  Accepts CRLF or LF line ends. */
+mst_status mst_mesh_read_msh(const char *path, mst_mesh **out);
+
+typedef struct mst_mesh_desc {
+  int n_nodes;
+  const double *node_xy;  /* [n_nodes][2] */
+  int n_cells;
+  int n_faces;
+  const int *face_nodes;  /* [n_faces][2], 0-based */
+  const int *face_cells;  /* [n_faces][2], c1 = -1 on boundary faces */
+  int n_zones;
+  const int *zones;       /* [n_zones][4]: id, first face (1-based), last, type */
+  /* Optional periodic images: [n_faces][2] translation that maps cell c1's
+   * coordinates into the frame of the face (zero for ordinary faces); NULL
+   * for none.  Periodic faces are interior faces (zone type 2). */
+  const double *c1_shift;
+} mst_mesh_desc;
+
+/* Builds a mesh from raw arrays (same geometry rules as mst_mesh_read_msh);
+ * replaces MshBlock::dataToMesh2D for generated meshes. */
+mst_status mst_mesh_create(const mst_mesh_desc *desc, mst_mesh **out);
+void mst_mesh_destroy(mst_mesh *m);
+
+typedef struct mst_mesh_info {
+  int n_nodes, n_cells, n_faces, n_int_faces, n_zones, n_cell_faces;
+  int n_inner, n_bond1, n_bond2; /* MshBlock boundary lists (:370-406) */
+  int n_tiles;                   /* device cell tiles */
+} mst_mesh_info;
+mst_status mst_mesh_get_info(const mst_mesh *m, mst_mesh_info *info);
+
+/* Exports the host geometry in file numbering, for parity checks; every
+ * pointer may be NULL.  Sizes follow mst_mesh_info.  face_flag holds the
+ * reference's flagLeftRight as 0/1 bytes [n_faces][2]. */
+typedef struct mst_mesh_arrays {
+  double *face_ctr, *face_dir, *face_area, *face_eta0; /* [nF][2],[nF][2],[nF],[nF] */
+  int *face_dac;                                       /* [nF] */
+  uint8_t *face_flag;                                  /* [nF][2] */
+  int *face_cells;                                     /* [nF][2] */
+  int *cell_ptr, *cell_faces, *cell_nb;                /* CSR, file order */
+  double *cell_dof, *cell_eta0c;                       /* [tot][2], [tot] */
+  double *cell_ctr, *cell_vol;                         /* [nC][2], [nC] */
+  int *inner, *bond1, *bond2;
+  int *cell_perm;   /* [nC] device slot of each file-numbered cell */
+  int *face_perm;   /* [nF] device slot of each file-numbered face */
+} mst_mesh_arrays;
+mst_status mst_mesh_get_arrays(const mst_mesh *m, mst_mesh_arrays *a);
+
+/* ------------------------------------------------------------------ */
+/* solver contexts: the RhoSolver surface                              */
+/* ------------------------------------------------------------------ */
+typedef struct mst_ctx mst_ctx;
+
+/* RhoSolver(MshBlock*, fstream*, AllData*) (RhoSolver.h:17): uploads the
+ * mesh once and allocates the device state.  The mesh must outlive it. */
+mst_status mst_ctx_create(const mst_mesh *m, const mst_params *p,
+                          mst_ctx **out);
+mst_status mst_ctx_destroy(mst_ctx *c);
+/* Replaces the parameters (the mesh stays resident). */
+mst_status mst_ctx_set_params(mst_ctx *c, const mst_params *p);
+
+/* RhoSolver::setDT (RhoSolver.cpp:33-35). */
+mst_status mst_set_dt(mst_ctx *c, double dt);
+
+/* Old state in (AllData p1OldCellQs, the Q that solve() reads). */
+mst_status mst_set_state(mst_ctx *c, const double *q, size_t stride);
+/* getOldValue (RhoSolver.cpp:504-506). */
+mst_status mst_get_state(mst_ctx *c, double *q, size_t stride);
+/* getNewValue (RhoSolver.cpp:507-509): the state solve() produced. */
+mst_status mst_get_new_state(mst_ctx *c, double *q, size_t stride);
+
+/* RhoSolver::solve (RhoSolver.cpp:37-89): one residual evaluation and one
+ * explicit update Qnew = Qold - DT/V*R into the new-state buffer. */
+mst_status mst_solve(mst_ctx *c);
+/* RhoSolver::updateNewToOld (RhoSolver.cpp:513-517). */
+mst_status mst_update_new_to_old(mst_ctx *c);
+
+/* Per-cell residual R of the last solve(), [n_cells][4] (the reference's
+ * integralConvectFlux, RhoSolver.cpp:47-56). */
+mst_status mst_get_residual(mst_ctx *c, double *r, size_t stride);
+/* Per-face flux matrices of the last solve(), [n_faces][2][4]
+ * (p1OldFaceConvectFlux, RhoSolver.cpp:90-369). */
+mst_status mst_get_face_flux(mst_ctx *c, double *f);
+/* Cell gradients of the last 2nd-order solve(), [n_cells][2][4]
+ * (p1NewCellGradFlux, RhoSolver.cpp:430-453). */
+mst_status mst_get_gradient(mst_ctx *c, double *g);
+
+/* Norms of one step. */
+typedef struct mst_norms {
+  double linf_change[4]; /* Time::goNextTimeStep, time/Time.cpp:69-76 */
+  double l2_resid[4];    /* sqrt(sum_c (R_c/V_c)^2 / n_cells) */
+  double dt;             /* step actually taken */
+  double time;           /* simulated time after the step */
+  double mass;           /* sum_c V_c * rho_c (conservation check) */
+} mst_norms;
+
+/* Device-resident time stepping: nsteps steps of the configured scheme
+ * without host round trips (the Work::work loop, work/Work.cpp:53-89, with
+ * the state kept in HBM).  t_end > 0 clips the last step to reach t_end
+ * exactly.  last (nullable) receives the norms of the final step. */
+mst_status mst_step(mst_ctx *c, int nsteps, double t_end, mst_norms *last);
+
+/* Simulated time of the context (sum of the steps taken). */
+mst_status mst_get_time(mst_ctx *c, double *t);
+
+/* Launch-level timing of the most recent mst_step/mst_solve on the
+ * context's stream: elapsed milliseconds between its first and last
+ * kernel, and the number of kernels launched. */
+mst_status mst_last_timing(mst_ctx *c, double *ms, int *launches);
+
+/* Text of the last error on this thread (static storage). */
+const char *mst_last_error(void);
+/* ABI version. */
+int mst_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

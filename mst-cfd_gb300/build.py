@@ -1,0 +1,89 @@
+"""Builds the in-tree CUDA library ``mst-cfd_gb300/lib/libmstcfd.so``.
+
+Translation units are compiled in parallel for sm_103a only:
+  * csrc/mesh.cpp          host mesh front end (g++, -ffp-contract=off so the
+                           geometry rounds like the reference on any host)
+  * csrc/kernels_exact.cu  FP64 parity kernels, --fmad=false
+  * csrc/kernels_fast.cu   FP64/FP32 production kernels (FMA allowed)
+  * csrc/capi.cu           the C ABI of include/mstcfd.h
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIBDIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIBDIR, "libmstcfd.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _units():
+    nv = _nvcc()
+    common = ["-O3", "-std=c++17", "-lineinfo", "-I", INCLUDE,
+              "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH
+    return [
+        ("mesh.o", ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                    "-Wall", "-c", os.path.join(CSRC, "mesh.cpp")]),
+        ("kernels_exact.o", [nv] + common + ["--fmad=false", "-c",
+                                             os.path.join(CSRC, "kernels_exact.cu")]),
+        ("kernels_fast.o", [nv] + common + ["-c", os.path.join(CSRC, "kernels_fast.cu")]),
+        ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
+    ]
+
+
+def _deps():
+    out = []
+    for d in (CSRC, INCLUDE):
+        for f in os.listdir(d):
+            out.append(os.path.join(d, f))
+    return out + [os.path.abspath(__file__)]
+
+
+def build(force=False, verbose=False):
+    """Compile (if stale) and return the path of libmstcfd.so."""
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(p) <= t for p in _deps()):
+            return LIB
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    units = _units()
+
+    def run(u):
+        name, cmd = u
+        cmd = cmd + ["-o", os.path.join(OBJ, name)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return name, r.returncode, r.stdout + r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        results = list(ex.map(run, units))
+    for name, rc, out in results:
+        if verbose or rc:
+            sys.stderr.write(f"--- {name} (rc={rc})\n{out}\n")
+        if rc:
+            raise RuntimeError(f"compiling {name} failed")
+    tmp = LIB + ".tmp"
+    link = [_nvcc(), "-shared"] + ARCH + ["-o", tmp] + \
+        [os.path.join(OBJ, n) for n, _ in units]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("linking libmstcfd.so failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

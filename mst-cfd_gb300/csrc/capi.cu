@@ -1,0 +1,707 @@
+// C ABI of the GB300 density-based residual path (include/mstcfd.h).
+// No exception crosses the boundary; every CUDA error becomes MST_ECUDA with
+// its text in mst_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mstcfd.h"
+#include "devtypes.hpp"
+#include "mesh.hpp"
+
+using mst::kNormSlots;
+
+namespace {
+
+thread_local std::string g_err;
+
+mst_status fail(mst_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+#define CU(call)                                                          \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      return fail(MST_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  *dst = nullptr;
+  size_t n = std::max<size_t>(src.size(), 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)dst, n);
+  if (e != cudaSuccess) return e;
+  if (!src.empty()) e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
+// ---- small orchestration kernels (not on the arithmetic-parity path) ----
+// device state -> file order and back
+__global__ void k_gather_rows(const double4_32a* __restrict__ src,
+                              const int* __restrict__ idx,
+                              double4_32a* __restrict__ dst, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[idx[i]];
+}
+
+// step length: fixed (mode 0) or min over block partials (mode 1), clipped
+// so that the time reaches t_end; writes scal[0] = dt
+__global__ void k_finalize_dt(const double* __restrict__ part, int n,
+                              int mode, double dt_fixed, double t_end,
+                              double* __restrict__ scal) {
+  __shared__ double red[32];
+  double x = 1e300;
+  if (mode == 0) {
+    x = dt_fixed;
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x = (part[i] < x) ? part[i] : x;
+    for (int o = 16; o > 0; o >>= 1) {
+      double w = __shfl_xor_sync(0xffffffffu, x, o);
+      x = (w < x) ? w : x;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      x = red[0];
+      for (int i = 1; i < (int)(blockDim.x >> 5); ++i) x = (red[i] < x) ? red[i] : x;
+    }
+  }
+  if (threadIdx.x == 0) {
+    double t = scal[1];
+    if (t_end > 0 && t + x > t_end) x = t_end - t;
+    if (x < 0) x = 0;
+    scal[0] = x;
+  }
+}
+
+// norms of a step from per-tile partials (fixed order: deterministic);
+// advances the simulated time by scal[0] when advance != 0.
+// out: linf[4], l2[4] (sqrt(mean)), mass, dt, time
+__global__ void k_finalize_norms(const double* __restrict__ part, int n_tiles,
+                                 int n_cells, int advance,
+                                 double* __restrict__ scal,
+                                 double* __restrict__ out) {
+  __shared__ double red[kNormSlots][32];
+  const int j = threadIdx.y;  // one row of threads per norm slot
+  double x = 0.0;
+  for (int i = threadIdx.x; i < n_tiles; i += blockDim.x) {
+    double v = part[(size_t)i * kNormSlots + j];
+    x = (j < 4) ? ((x < v) ? v : x) : x + v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, x, o);
+    x = (j < 4) ? ((x < w) ? w : x) : x + w;
+  }
+  if ((threadIdx.x & 31) == 0) red[j][threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double acc = red[j][0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i)
+      acc = (j < 4) ? ((acc < red[j][i]) ? red[j][i] : acc) : acc + red[j][i];
+    if (j >= 4 && j < 8) acc = sqrt(acc / (double)n_cells);
+    out[j] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && j == 0) {
+    if (advance) scal[1] += scal[0];
+    out[kNormSlots] = scal[0];
+    out[kNormSlots + 1] = scal[1];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct mst_mesh {
+  mst::HostMesh host;
+  mst::DevLayout lay;
+};
+
+struct DevArrays {
+  int2* f_c0c1 = nullptr;
+  int* f_info = nullptr;
+  double2 *f_dir = nullptr, *f_r0 = nullptr, *f_r1 = nullptr, *cf_w = nullptr;
+  float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr;
+  double* c_vol = nullptr;
+  int *c_ptr = nullptr, *cf_face = nullptr, *cf_slot = nullptr, *cf_nb = nullptr,
+      *cf_nb_fix = nullptr, *t_own_ptr = nullptr, *t_bor_ptr = nullptr,
+      *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr;
+};
+
+struct mst_ctx {
+  const mst_mesh* mesh = nullptr;
+  mst_params p{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevArrays d;
+  mst::DevMesh dm{};
+  double4_32a *q_old = nullptr, *q_new = nullptr, *q_stage = nullptr,
+              *r = nullptr, *stage_in = nullptr;
+  void* grad = nullptr;
+  double* flux = nullptr;      // [nF][8] debug output
+  double* partials = nullptr;  // [max(nT, nBlocks)][kNormSlots]
+  double* dt_part = nullptr;   // [nBlocks]
+  double* dt_cell = nullptr;   // [nC]
+  double* scal = nullptr;      // [0] dt, [1] time
+  double* norms = nullptr;     // [kNormSlots + 2]
+  int last_launches = 0;
+  bool timed = false;
+  bool grad_valid = false;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int prec_of(const mst_params& p) { return p.precision; }
+
+mst_status check_params(const mst_params* p) {
+  if (!p) return fail(MST_EINVAL, "params is NULL");
+  if (p->flux != MST_FLUX_AUSM && p->flux != MST_FLUX_ROE)
+    return fail(MST_EINVAL, "unknown flux scheme");
+  if (p->order != 1 && p->order != 2) return fail(MST_EINVAL, "order must be 1 or 2");
+  if (p->limiter < MST_LIMITER_NONE || p->limiter > MST_LIMITER_VANALBADA)
+    return fail(MST_EINVAL, "unknown limiter");
+  if (p->precision < MST_PREC_FP64_EXACT || p->precision > MST_PREC_FP32)
+    return fail(MST_EINVAL, "unknown precision");
+  if (p->time_scheme != MST_TIME_EULER && p->time_scheme != MST_TIME_RK2)
+    return fail(MST_EINVAL, "unknown time scheme");
+  if (p->dt_mode < MST_DT_FIXED || p->dt_mode > MST_DT_CFL_LOCAL)
+    return fail(MST_EINVAL, "unknown dt mode");
+  if (p->dt_mode == MST_DT_FIXED && !(p->dt >= 0))
+    return fail(MST_EINVAL, "dt must be >= 0");
+  if (p->dt_mode != MST_DT_FIXED && !(p->cfl > 0))
+    return fail(MST_EINVAL, "cfl must be > 0");
+  return MST_OK;
+}
+
+mst_status launch_grad(mst_ctx* c, const double4_32a* q) {
+  cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
+                      ? mst::exact::launch_gradient(prec_of(c->p), c->dm, q, c->grad,
+                                                    c->p.reference_quirks, c->stream)
+                      : mst::fast::launch_gradient(prec_of(c->p), c->dm, q, c->grad,
+                                                   c->p.reference_quirks, c->stream);
+  c->last_launches++;
+  if (e != cudaSuccess) return fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
+  c->grad_valid = true;
+  return MST_OK;
+}
+
+mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
+  cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
+                      ? mst::exact::launch_flux_update(prec_of(c->p), c->p.flux, c->p.order,
+                                                       c->dm, a, 0, c->stream)
+                      : mst::fast::launch_flux_update(prec_of(c->p), c->p.flux, c->p.order,
+                                                      c->dm, a, 0, c->stream);
+  c->last_launches++;
+  if (e != cudaSuccess) return fail(MST_ECUDA, std::string("flux_update: ") + cudaGetErrorString(e));
+  return MST_OK;
+}
+
+mst::StepArgs base_args(mst_ctx* c) {
+  mst::StepArgs a{};
+  a.grad = c->grad;
+  a.dt = c->p.dt;
+  a.quirks = c->p.reference_quirks;
+  a.limiter = c->p.limiter;
+  for (int k = 0; k < 4; ++k) a.inlet[k] = c->p.inlet_q[k];
+  return a;
+}
+
+// one residual evaluation + update of stage 'stage' from q into qn
+mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
+                     double4_32a* qn, int stage, bool fixed_dt, bool norms) {
+  if (c->p.order == 2) {
+    mst_status s = launch_grad(c, q);
+    if (s) return s;
+  }
+  mst::StepArgs a = base_args(c);
+  a.q = q;
+  a.q0 = q0;
+  a.qn = qn;
+  a.r_out = c->r;
+  a.stage = stage;
+  if (!fixed_dt) {
+    if (c->p.dt_mode == MST_DT_CFL_LOCAL) a.dt_cell = c->dt_cell;
+    else a.dt_dev = c->scal;
+  }
+  a.partials = norms ? c->partials : nullptr;
+  return launch_flux(c, a);
+}
+
+mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end) {
+  const int nC = c->dm.n_cells;
+  int mode = 0;
+  if (c->p.dt_mode != MST_DT_FIXED) {
+    cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
+                        ? mst::exact::launch_spectral_dt(prec_of(c->p), c->dm, q, c->p.cfl,
+                                                         c->dt_cell, c->dt_part, c->stream)
+                        : mst::fast::launch_spectral_dt(prec_of(c->p), c->dm, q, c->p.cfl,
+                                                        c->dt_cell, c->dt_part, c->stream);
+    c->last_launches++;
+    if (e != cudaSuccess) return fail(MST_ECUDA, std::string("spectral_dt: ") + cudaGetErrorString(e));
+    mode = 1;
+  }
+  k_finalize_dt<<<1, 1024, 0, c->stream>>>(c->dt_part, (nC + 255) / 256, mode, c->p.dt,
+                                            t_end, c->scal);
+  c->last_launches++;
+  CU(cudaGetLastError());
+  return MST_OK;
+}
+
+mst_status finalize_norms(mst_ctx* c, bool advance) {
+  k_finalize_norms<<<1, dim3(64, kNormSlots), 0, c->stream>>>(
+      c->partials, c->dm.n_tiles, c->dm.n_cells, advance ? 1 : 0, c->scal, c->norms);
+  c->last_launches++;
+  CU(cudaGetLastError());
+  return MST_OK;
+}
+
+mst_status read_norms(mst_ctx* c, mst_norms* out) {
+  double h[kNormSlots + 2];
+  CU(cudaMemcpyAsync(h, c->norms, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  if (out) {
+    for (int j = 0; j < 4; ++j) {
+      out->linf_change[j] = h[j];
+      out->l2_resid[j] = h[4 + j];
+    }
+    out->mass = h[8];
+    out->dt = h[kNormSlots];
+    out->time = h[kNormSlots + 1];
+  }
+  return MST_OK;
+}
+
+template <class T>
+mst_status dalloc(mst_ctx* c, T** p, size_t bytes) {
+  CU(cudaMalloc((void**)p, std::max<size_t>(bytes, 256)));
+  c->allocs.push_back(*p);
+  return MST_OK;
+}
+
+mst_status download_rows(mst_ctx* c, const double4_32a* dev, double* host,
+                         size_t stride) {
+  const int nC = c->dm.n_cells;
+  // device order -> file order with a gather by cell_perm, then one copy
+  k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(dev, c->d.cell_perm, c->stage_in, nC);
+  CU(cudaGetLastError());
+  CU(cudaMemcpy2DAsync(host, stride * sizeof(double), c->stage_in, 4 * sizeof(double),
+                       4 * sizeof(double), nC, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return MST_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* mst_last_error(void) { return g_err.c_str(); }
+int mst_abi_version(void) { return MSTCFD_ABI_VERSION; }
+
+void mst_params_default(mst_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->flux = MST_FLUX_AUSM;
+  p->order = 1;
+  p->limiter = MST_LIMITER_NONE;
+  p->precision = MST_PREC_FP64_EXACT;
+  p->time_scheme = MST_TIME_EULER;
+  p->dt_mode = MST_DT_FIXED;
+  p->dt = 1.0 / 4e+3;  // 1/STEP_TIME (CONST.h:52, Time.cpp:62)
+  p->cfl = 0.5;
+  // CONST.h:70-83 as the macros expand: rho 1, u = v = 0, E = 1/286.32*715.8
+  p->inlet_q[0] = 1;
+  p->inlet_q[1] = 1.0 * 0;
+  p->inlet_q[2] = 1.0 * 0;
+  p->inlet_q[3] = 1 * (1 / 286.32 * 715.8 + 0.5 * (0 * 0 + 0 * 0));
+  p->reference_quirks = 1;
+}
+
+mst_status mst_mesh_read_msh(const char* path, mst_mesh** out) {
+  if (!path || !out) return fail(MST_EINVAL, "NULL argument");
+  *out = nullptr;
+  try {
+    std::unique_ptr<mst_mesh> m(new mst_mesh);
+    std::string err;
+    int rc = mst::read_msh(path, &m->host, &err);
+    if (rc) return fail(rc == mst::kEInval ? MST_EINVAL : MST_EMESH, err);
+    rc = mst::build_layout(m->host, true, &m->lay, &err);
+    if (rc) return fail(MST_EMESH, err);
+    *out = m.release();
+    return MST_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MST_ENOMEM, "host allocation failed");
+  } catch (...) {
+    return fail(MST_EMESH, "mesh read failed");
+  }
+}
+
+mst_status mst_mesh_create(const mst_mesh_desc* d, mst_mesh** out) {
+  if (!d || !out) return fail(MST_EINVAL, "NULL argument");
+  *out = nullptr;
+  try {
+    std::unique_ptr<mst_mesh> m(new mst_mesh);
+    std::string err;
+    int rc = mst::build_from_arrays(d->n_nodes, d->node_xy, d->n_cells, d->n_faces,
+                                    d->face_nodes, d->face_cells, d->n_zones, d->zones,
+                                    d->c1_shift, &m->host, &err);
+    if (rc) return fail(rc == mst::kEInval ? MST_EINVAL : MST_EMESH, err);
+    rc = mst::build_layout(m->host, true, &m->lay, &err);
+    if (rc) return fail(MST_EMESH, err);
+    *out = m.release();
+    return MST_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MST_ENOMEM, "host allocation failed");
+  } catch (...) {
+    return fail(MST_EMESH, "mesh build failed");
+  }
+}
+
+void mst_mesh_destroy(mst_mesh* m) { delete m; }
+
+mst_status mst_mesh_get_info(const mst_mesh* m, mst_mesh_info* info) {
+  if (!m || !info) return fail(MST_EINVAL, "NULL argument");
+  const auto& h = m->host;
+  info->n_nodes = h.n_nodes;
+  info->n_cells = h.n_cells;
+  info->n_faces = h.n_faces;
+  info->n_int_faces = h.n_int_faces;
+  info->n_zones = h.n_zones();
+  info->n_cell_faces = h.cell_ptr.empty() ? 0 : h.cell_ptr.back();
+  info->n_inner = (int)h.inner.size();
+  info->n_bond1 = (int)h.bond1.size();
+  info->n_bond2 = (int)h.bond2.size();
+  info->n_tiles = m->lay.n_tiles;
+  return MST_OK;
+}
+
+mst_status mst_mesh_get_arrays(const mst_mesh* m, mst_mesh_arrays* a) {
+  if (!m || !a) return fail(MST_EINVAL, "NULL argument");
+  const auto& h = m->host;
+  auto cp = [](auto* dst, const auto& v) {
+    if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+  };
+  cp(a->face_ctr, h.face_ctr);
+  cp(a->face_dir, h.face_dir);
+  cp(a->face_area, h.face_area);
+  cp(a->face_eta0, h.face_eta0);
+  cp(a->face_dac, h.face_dac);
+  cp(a->face_flag, h.face_flag);
+  cp(a->face_cells, h.face_cells);
+  cp(a->cell_ptr, h.cell_ptr);
+  cp(a->cell_faces, h.cell_faces);
+  cp(a->cell_nb, h.cell_nb);
+  cp(a->cell_dof, h.cell_dof);
+  cp(a->cell_eta0c, h.cell_eta0c);
+  cp(a->cell_ctr, h.cell_ctr);
+  cp(a->cell_vol, h.cell_vol);
+  cp(a->inner, h.inner);
+  cp(a->bond1, h.bond1);
+  cp(a->bond2, h.bond2);
+  cp(a->cell_perm, m->lay.cell_perm);
+  cp(a->face_perm, m->lay.face_perm);
+  return MST_OK;
+}
+
+mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out) {
+  if (!m || !out) return fail(MST_EINVAL, "NULL argument");
+  *out = nullptr;
+  mst_status st = check_params(p);
+  if (st) return st;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(MST_ECUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  std::unique_ptr<mst_ctx> c(new (std::nothrow) mst_ctx);
+  if (!c) return fail(MST_ENOMEM, "host allocation failed");
+  c->mesh = m;
+  c->p = *p;
+  CU(cudaGetDevice(&c->device));
+  CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&c->ev0));
+  CU(cudaEventCreate(&c->ev1));
+  const auto& L = m->lay;
+  DevArrays& d = c->d;
+  auto up = [&](auto** dst, const auto& v) -> cudaError_t {
+    cudaError_t r = upload(dst, v);
+    c->allocs.push_back((void*)*dst);
+    return r;
+  };
+  {
+    std::vector<int2> c0c1(L.n_faces);
+    for (int i = 0; i < L.n_faces; ++i) c0c1[i] = make_int2(L.f_c0c1[2 * i], L.f_c0c1[2 * i + 1]);
+    auto as_d2 = [](const std::vector<double>& v) {
+      std::vector<double2> o(v.size() / 2);
+      for (size_t i = 0; i < o.size(); ++i) o[i] = make_double2(v[2 * i], v[2 * i + 1]);
+      return o;
+    };
+    auto as_f2 = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size() / 2);
+      for (size_t i = 0; i < o.size(); ++i) o[i] = make_float2((float)v[2 * i], (float)v[2 * i + 1]);
+      return o;
+    };
+    CU(up(&d.f_c0c1, c0c1));
+    CU(up(&d.f_info, L.f_info));
+    CU(up(&d.f_dir, as_d2(L.f_dir)));
+    CU(up(&d.f_r0, as_d2(L.f_r0)));
+    CU(up(&d.f_r1, as_d2(L.f_r1)));
+    CU(up(&d.cf_w, as_d2(L.cf_w)));
+    CU(up(&d.f_dir32, as_f2(L.f_dir)));
+    CU(up(&d.f_r0_32, as_f2(L.f_r0)));
+    CU(up(&d.f_r1_32, as_f2(L.f_r1)));
+    CU(up(&d.cf_w32, as_f2(L.cf_w)));
+    CU(up(&d.c_vol, L.c_vol));
+    CU(up(&d.c_ptr, L.c_ptr));
+    CU(up(&d.cf_face, L.cf_face));
+    CU(up(&d.cf_slot, L.cf_slot));
+    CU(up(&d.cf_nb, L.cf_nb));
+    CU(up(&d.cf_nb_fix, L.cf_nb_fix));
+    CU(up(&d.t_own_ptr, L.t_own_ptr));
+    CU(up(&d.t_bor_ptr, L.t_bor_ptr));
+    CU(up(&d.t_bor, L.t_bor));
+    CU(up(&d.cell_iperm, L.cell_iperm));
+    CU(up(&d.cell_perm, L.cell_perm));
+  }
+  mst::DevMesh& dm = c->dm;
+  dm.n_cells = L.n_cells;
+  dm.n_faces = L.n_faces;
+  dm.n_tiles = L.n_tiles;
+  dm.max_tile_faces = L.max_tile_faces;
+  dm.f_c0c1 = d.f_c0c1;
+  dm.f_info = d.f_info;
+  dm.f_dir = d.f_dir;
+  dm.f_r0 = d.f_r0;
+  dm.f_r1 = d.f_r1;
+  dm.f_dir32 = d.f_dir32;
+  dm.f_r0_32 = d.f_r0_32;
+  dm.f_r1_32 = d.f_r1_32;
+  dm.c_vol = d.c_vol;
+  dm.c_ptr = d.c_ptr;
+  dm.cf_face = d.cf_face;
+  dm.cf_slot = d.cf_slot;
+  dm.cf_nb = d.cf_nb;
+  dm.cf_nb_fix = d.cf_nb_fix;
+  dm.cf_w = d.cf_w;
+  dm.cf_w32 = d.cf_w32;
+  dm.t_own_ptr = d.t_own_ptr;
+  dm.t_bor_ptr = d.t_bor_ptr;
+  dm.t_bor = d.t_bor;
+  const size_t nC = L.n_cells, nB = (nC + 255) / 256;
+  const size_t qbytes = nC * sizeof(double4_32a);
+  if ((st = dalloc(c.get(), &c->q_old, qbytes)) || (st = dalloc(c.get(), &c->q_new, qbytes)) ||
+      (st = dalloc(c.get(), &c->q_stage, qbytes)) || (st = dalloc(c.get(), &c->r, qbytes)) ||
+      (st = dalloc(c.get(), &c->stage_in, qbytes)) ||
+      (st = dalloc(c.get(), (char**)&c->grad, nC * 8 * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->partials,
+                   std::max<size_t>(L.n_tiles, nB) * kNormSlots * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->dt_part, nB * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->dt_cell, nC * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->scal, 4 * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->norms, (kNormSlots + 2) * sizeof(double))))
+    return st;
+  CU(cudaMemset(c->q_old, 0, qbytes));
+  CU(cudaMemset(c->q_new, 0, qbytes));
+  CU(cudaMemset(c->r, 0, qbytes));
+  CU(cudaMemset(c->scal, 0, 4 * sizeof(double)));
+  CU(cudaMemset(c->norms, 0, (kNormSlots + 2) * sizeof(double)));
+  CU(cudaDeviceSynchronize());
+  *out = c.release();
+  return MST_OK;
+}
+
+mst_status mst_ctx_destroy(mst_ctx* c) {
+  if (!c) return MST_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MST_OK;
+}
+
+mst_status mst_ctx_set_params(mst_ctx* c, const mst_params* p) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  mst_status st = check_params(p);
+  if (st) return st;
+  c->p = *p;
+  c->grad_valid = false;
+  return MST_OK;
+}
+
+mst_status mst_set_dt(mst_ctx* c, double dt) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  if (!(dt >= 0)) return fail(MST_EINVAL, "dt must be >= 0");
+  c->p.dt = dt;
+  return MST_OK;
+}
+
+mst_status mst_set_state(mst_ctx* c, const double* q, size_t stride) {
+  if (!c || !q) return fail(MST_EINVAL, "NULL argument");
+  if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  const int nC = c->dm.n_cells;
+  CU(cudaMemcpy2DAsync(c->stage_in, 4 * sizeof(double), q, stride * sizeof(double),
+                       4 * sizeof(double), nC, cudaMemcpyHostToDevice, c->stream));
+  k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(c->stage_in, c->d.cell_iperm,
+                                                           c->q_old, nC);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(c->q_new, c->q_old, (size_t)nC * sizeof(double4_32a),
+                     cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  c->grad_valid = false;
+  return MST_OK;
+}
+
+mst_status mst_get_state(mst_ctx* c, double* q, size_t stride) {
+  if (!c || !q) return fail(MST_EINVAL, "NULL argument");
+  if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  return download_rows(c, c->q_old, q, stride);
+}
+
+mst_status mst_get_new_state(mst_ctx* c, double* q, size_t stride) {
+  if (!c || !q) return fail(MST_EINVAL, "NULL argument");
+  if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  return download_rows(c, c->q_new, q, stride);
+}
+
+mst_status mst_get_residual(mst_ctx* c, double* r, size_t stride) {
+  if (!c || !r) return fail(MST_EINVAL, "NULL argument");
+  if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  return download_rows(c, c->r, r, stride);
+}
+
+mst_status mst_solve(mst_ctx* c) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  c->last_launches = 0;
+  CU(cudaEventRecord(c->ev0, c->stream));
+  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true);
+  if (s) return s;
+  if ((s = finalize_norms(c, false))) return s;
+  CU(cudaEventRecord(c->ev1, c->stream));
+  c->timed = true;
+  CU(cudaStreamSynchronize(c->stream));
+  return MST_OK;
+}
+
+mst_status mst_update_new_to_old(mst_ctx* c) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  CU(cudaMemcpyAsync(c->q_old, c->q_new, (size_t)c->dm.n_cells * sizeof(double4_32a),
+                     cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  c->grad_valid = false;
+  return MST_OK;
+}
+
+mst_status mst_get_face_flux(mst_ctx* c, double* f) {
+  if (!c || !f) return fail(MST_EINVAL, "NULL argument");
+  const int nF = c->dm.n_faces;
+  if (!c->flux) {
+    mst_status s = dalloc(c, &c->flux, (size_t)nF * 8 * sizeof(double));
+    if (s) return s;
+  }
+  if (c->p.order == 2 && !c->grad_valid) {
+    mst_status s = launch_grad(c, c->q_old);
+    if (s) return s;
+  }
+  mst::StepArgs a = base_args(c);
+  a.q = c->q_old;
+  cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
+                      ? mst::exact::launch_face_flux(prec_of(c->p), c->p.flux, c->p.order, c->dm, a,
+                                                     c->flux, c->stream)
+                      : mst::fast::launch_face_flux(prec_of(c->p), c->p.flux, c->p.order, c->dm, a,
+                                                    c->flux, c->stream);
+  if (e != cudaSuccess) return fail(MST_ECUDA, std::string("face_flux: ") + cudaGetErrorString(e));
+  std::vector<double> h((size_t)nF * 8);
+  CU(cudaMemcpyAsync(h.data(), c->flux, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  const auto& L = c->mesh->lay;
+  for (int i = 0; i < nF; ++i)
+    std::memcpy(f + 8 * (size_t)i, h.data() + 8 * (size_t)L.face_perm[i], 8 * sizeof(double));
+  return MST_OK;
+}
+
+mst_status mst_get_gradient(mst_ctx* c, double* g) {
+  if (!c || !g) return fail(MST_EINVAL, "NULL argument");
+  if (c->p.order != 2) return fail(MST_EINVAL, "gradients exist for order 2 only");
+  if (!c->grad_valid) {
+    mst_status s = launch_grad(c, c->q_old);
+    if (s) return s;
+  }
+  const int nC = c->dm.n_cells;
+  const auto& L = c->mesh->lay;
+  if (c->p.precision == MST_PREC_FP32) {
+    std::vector<float> h((size_t)nC * 8);
+    CU(cudaMemcpyAsync(h.data(), c->grad, h.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nC; ++i)
+      for (int k = 0; k < 8; ++k) g[8 * (size_t)i + k] = h[8 * (size_t)L.cell_perm[i] + k];
+  } else {
+    std::vector<double> h((size_t)nC * 8);
+    CU(cudaMemcpyAsync(h.data(), c->grad, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nC; ++i)
+      std::memcpy(g + 8 * (size_t)i, h.data() + 8 * (size_t)L.cell_perm[i], 8 * sizeof(double));
+  }
+  return MST_OK;
+}
+
+mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  if (nsteps < 0) return fail(MST_EINVAL, "nsteps must be >= 0");
+  c->last_launches = 0;
+  CU(cudaEventRecord(c->ev0, c->stream));
+  for (int s = 0; s < nsteps; ++s) {
+    mst_status st = compute_dt(c, c->q_old, t_end);
+    if (st) return st;
+    if (c->p.time_scheme == MST_TIME_EULER) {
+      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, true);
+    } else {
+      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false);
+      if (!st) st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, true);
+    }
+    if (st) return st;
+    if ((st = finalize_norms(c, true))) return st;
+    std::swap(c->q_old, c->q_new);
+  }
+  CU(cudaEventRecord(c->ev1, c->stream));
+  c->timed = true;
+  c->grad_valid = false;
+  if (last) return read_norms(c, last);
+  CU(cudaStreamSynchronize(c->stream));
+  return MST_OK;
+}
+
+mst_status mst_get_time(mst_ctx* c, double* t) {
+  if (!c || !t) return fail(MST_EINVAL, "NULL argument");
+  double h[4];
+  CU(cudaMemcpyAsync(h, c->scal, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  *t = h[1];
+  return MST_OK;
+}
+
+mst_status mst_last_timing(mst_ctx* c, double* ms, int* launches) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  if (!c->timed) return fail(MST_EINVAL, "nothing timed yet");
+  CU(cudaEventSynchronize(c->ev1));
+  float f = 0;
+  CU(cudaEventElapsedTime(&f, c->ev0, c->ev1));
+  if (ms) *ms = f;
+  if (launches) *launches = c->last_launches;
+  return MST_OK;
+}
+
+}  // extern "C"

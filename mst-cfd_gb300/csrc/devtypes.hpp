@@ -1,0 +1,79 @@
+// Device-resident mesh and per-launch arguments shared by the kernel
+// translation units and the C ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mst {
+
+// Mesh arrays in device numbering (see mesh.hpp DevLayout).  Geometry is
+// held twice: FP64 for the exact and FP64 paths, FP32 for the FP32 path.
+struct DevMesh {
+  int n_cells, n_faces, n_tiles, max_tile_faces;
+  const int2* f_c0c1;
+  const int* f_info;
+  const double2* f_dir;
+  const double2* f_r0;
+  const double2* f_r1;
+  const float2* f_dir32;
+  const float2* f_r0_32;
+  const float2* f_r1_32;
+  const double* c_vol;
+  const int* c_ptr;
+  const int* cf_face;
+  const int* cf_slot;
+  const int* cf_nb;
+  const int* cf_nb_fix;
+  const double2* cf_w;
+  const float2* cf_w32;
+  const int* t_own_ptr;
+  const int* t_bor_ptr;
+  const int* t_bor;
+};
+
+// Number of doubles of per-tile partial norms: linf[4], l2[4], mass.
+constexpr int kNormSlots = 9;
+
+struct StepArgs {
+  const double4_32a* q;   // state the residual is evaluated on
+  const double4_32a* q0;  // Q^n for the second RK stage (else nullptr)
+  double4_32a* qn;        // updated state
+  const void* grad;       // [n_cells][2][4] in the path's precision
+  double4_32a* r_out;     // optional per-cell residual
+  const double* dt_dev;   // device scalar step (CFL modes) or nullptr
+  const double* dt_cell;  // per-cell step (local CFL) or nullptr
+  double dt;              // fixed step
+  int stage;              // 0: Q - dt/V R;  1: 0.5 Q0 + 0.5 (Q - dt/V R)
+  int quirks;             // reproduce the reference's quirks
+  int limiter;            // MST_LIMITER_*
+  double inlet[4];
+  double* partials;       // [n_tiles][kNormSlots] or nullptr
+};
+
+// Precisions / schemes (mirrors of the public enums)
+enum { kPrecExact = 0, kPrecF64 = 1, kPrecF32 = 2 };
+enum { kFluxAusm = 0, kFluxRoe = 1 };
+
+// Launchers implemented once per arithmetic translation unit.
+#define MST_DECLARE_LAUNCHERS(NS)                                             \
+  namespace NS {                                                              \
+  cudaError_t launch_gradient(int prec, const DevMesh& m,                     \
+                              const double4_32a* q, void* grad, int quirks,   \
+                              cudaStream_t s);                                \
+  cudaError_t launch_flux_update(int prec, int flux, int order,              \
+                                 const DevMesh& m, const StepArgs& a,         \
+                                 int threads, cudaStream_t s);                \
+  cudaError_t launch_face_flux(int prec, int flux, int order,                \
+                               const DevMesh& m, const StepArgs& a,           \
+                               double* F, cudaStream_t s);                    \
+  cudaError_t launch_spectral_dt(int prec, const DevMesh& m,                 \
+                                 const double4_32a* q, double cfl,            \
+                                 double* dt_cell, double* partials,           \
+                                 cudaStream_t s);                             \
+  }
+
+MST_DECLARE_LAUNCHERS(exact)
+MST_DECLARE_LAUNCHERS(fast)
+
+}  // namespace mst

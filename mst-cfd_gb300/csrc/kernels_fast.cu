@@ -1,0 +1,37 @@
+// Production kernels: FP64 and FP32 reconstruction/flux with fused
+// multiply-add allowed; state, residual accumulation and norms stay FP64.
+#include "devtypes.hpp"
+#include "mesh.hpp"
+#include "physics.cuh"
+
+namespace mst {
+namespace fast {
+#include "kernels.inc"
+
+cudaError_t launch_gradient(int prec, const DevMesh& m, const double4_32a* q,
+                            void* grad, int quirks, cudaStream_t s) {
+  if (prec == kPrecF32) return gradient_t<float>(m, q, grad, quirks, s);
+  return gradient_t<double>(m, q, grad, quirks, s);
+}
+cudaError_t launch_flux_update(int prec, int flux, int order, const DevMesh& m,
+                               const StepArgs& a, int, cudaStream_t s) {
+  if (prec == kPrecF32) return flux_dispatch<float>(flux, order, m, a, s);
+  return flux_dispatch<double>(flux, order, m, a, s);
+}
+cudaError_t launch_face_flux(int prec, int flux, int order, const DevMesh& m,
+                             const StepArgs& a, double* F, cudaStream_t s) {
+  if (prec == kPrecF32) return face_dispatch<float>(flux, order, m, a, F, s);
+  return face_dispatch<double>(flux, order, m, a, F, s);
+}
+cudaError_t launch_spectral_dt(int prec, const DevMesh& m, const double4_32a* q,
+                               double cfl, double* dt_cell, double* partials,
+                               cudaStream_t s) {
+  const int nb = (m.n_cells + 255) / 256;
+  if (prec == kPrecF32)
+    k_spectral_dt<float><<<nb, 256, 0, s>>>(m, q, cfl, dt_cell, partials);
+  else
+    k_spectral_dt<double><<<nb, 256, 0, s>>>(m, q, cfl, dt_cell, partials);
+  return cudaGetLastError();
+}
+}  // namespace fast
+}  // namespace mst

@@ -1,0 +1,154 @@
+"""ctypes binding of the C ABI declared in include/mstcfd.h.
+
+Loads the in-tree ``lib/libmstcfd.so`` (building it first when it is missing
+and nvcc is available).  There is no fallback: if the library cannot be
+loaded, every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+
+OK, EINVAL, EMESH, ECUDA, EDIVERGED, ETIMEOUT, ENOMEM, EUNSUPPORTED = range(8)
+FLUX_AUSM, FLUX_ROE = 0, 1
+LIMITER_NONE, LIMITER_MINMOD, LIMITER_VANLEER, LIMITER_VANALBADA = range(4)
+PREC_FP64_EXACT, PREC_FP64, PREC_FP32 = range(3)
+TIME_EULER, TIME_RK2 = range(2)
+DT_FIXED, DT_CFL_GLOBAL, DT_CFL_LOCAL = range(3)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_uint8)
+
+
+class Params(C.Structure):
+    _fields_ = [("flux", C.c_int), ("order", C.c_int), ("limiter", C.c_int),
+                ("precision", C.c_int), ("time_scheme", C.c_int),
+                ("dt_mode", C.c_int), ("dt", C.c_double), ("cfl", C.c_double),
+                ("inlet_q", C.c_double * 4), ("reference_quirks", C.c_int),
+                ("reserved", C.c_int * 7)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("node_xy", _dp), ("n_cells", C.c_int),
+                ("n_faces", C.c_int), ("face_nodes", _ip), ("face_cells", _ip),
+                ("n_zones", C.c_int), ("zones", _ip), ("c1_shift", _dp)]
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [(n, C.c_int) for n in (
+        "n_nodes", "n_cells", "n_faces", "n_int_faces", "n_zones",
+        "n_cell_faces", "n_inner", "n_bond1", "n_bond2", "n_tiles")]
+
+
+class MeshArrays(C.Structure):
+    _fields_ = [("face_ctr", _dp), ("face_dir", _dp), ("face_area", _dp),
+                ("face_eta0", _dp), ("face_dac", _ip), ("face_flag", _up),
+                ("face_cells", _ip), ("cell_ptr", _ip), ("cell_faces", _ip),
+                ("cell_nb", _ip), ("cell_dof", _dp), ("cell_eta0c", _dp),
+                ("cell_ctr", _dp), ("cell_vol", _dp), ("inner", _ip),
+                ("bond1", _ip), ("bond2", _ip), ("cell_perm", _ip),
+                ("face_perm", _ip)]
+
+
+class Norms(C.Structure):
+    _fields_ = [("linf_change", C.c_double * 4), ("l2_resid", C.c_double * 4),
+                ("dt", C.c_double), ("time", C.c_double), ("mass", C.c_double)]
+
+
+class MstError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"mstcfd status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib_path():
+    return os.path.join(_PKG, "lib", "libmstcfd.so")
+
+
+def load():
+    """Load (building if needed) the CUDA library; raises on failure."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location(
+            "_mstcfd_build", os.path.join(_PKG, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = C.CDLL(path)
+    sigs = {
+        "mst_params_default": (None, [C.POINTER(Params)]),
+        "mst_mesh_read_msh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+        "mst_mesh_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
+        "mst_mesh_destroy": (None, [C.c_void_p]),
+        "mst_mesh_get_info": (C.c_int, [C.c_void_p, C.POINTER(MeshInfo)]),
+        "mst_mesh_get_arrays": (C.c_int, [C.c_void_p, C.POINTER(MeshArrays)]),
+        "mst_ctx_create": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(C.c_void_p)]),
+        "mst_ctx_destroy": (C.c_int, [C.c_void_p]),
+        "mst_ctx_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
+        "mst_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
+        "mst_set_state": (C.c_int, [C.c_void_p, _dp, C.c_size_t]),
+        "mst_get_state": (C.c_int, [C.c_void_p, _dp, C.c_size_t]),
+        "mst_get_new_state": (C.c_int, [C.c_void_p, _dp, C.c_size_t]),
+        "mst_solve": (C.c_int, [C.c_void_p]),
+        "mst_update_new_to_old": (C.c_int, [C.c_void_p]),
+        "mst_get_residual": (C.c_int, [C.c_void_p, _dp, C.c_size_t]),
+        "mst_get_face_flux": (C.c_int, [C.c_void_p, _dp]),
+        "mst_get_gradient": (C.c_int, [C.c_void_p, _dp]),
+        "mst_step": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(Norms)]),
+        "mst_get_time": (C.c_int, [C.c_void_p, _dp]),
+        "mst_last_timing": (C.c_int, [C.c_void_p, _dp, _ip]),
+        "mst_last_error": (C.c_char_p, []),
+        "mst_abi_version": (C.c_int, []),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != OK:
+        raise MstError(status, load().mst_last_error().decode(errors="replace"))
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip)
+
+
+def params(**kw):
+    """mst_params with the reference defaults, overridden by keywords."""
+    p = Params()
+    load().mst_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "inlet_q":
+            for i in range(4):
+                p.inlet_q[i] = float(v[i])
+        elif not hasattr(p, k):
+            raise KeyError(k)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a

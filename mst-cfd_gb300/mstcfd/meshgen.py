@@ -1,0 +1,345 @@
+"""Mesh generators, the Fluent .msh writer and initial states.
+
+Every generated face is oriented the way the reference's left/right logic
+needs (mesh/MshBlock.cpp:281-305): the area vector (-(y0-y1), x0-x1) of
+nodes (n0, n1) points INTO cell c0.  With that orientation the reference's
+flags and the geometric ones agree, so generated meshes upwind correctly
+with or without the reference's quirks.
+
+A mesh is a dict: node_xy [nN,2], face_nodes [nF,2], face_cells [nF,2]
+(c1 = -1 on boundary faces), zones [nz,4] = (id, first face 1-based, last,
+type), n_cells, and optionally c1_shift [nF,2] (periodic image shift).
+Zone types follow the reference: 2 interior, 3 wall, 5 outlet, 7 symmetry,
+10 inlet.
+"""
+import numpy as np
+
+GAMMA = 1.4
+INTERIOR, WALL, OUTLET, SYMMETRY, INLET = 2, 3, 5, 7, 10
+
+
+def _orient_into_c0(node_xy, face_nodes, face_cells, c0_point):
+    """Swap node order where the area vector does not point into c0."""
+    a = node_xy[face_nodes[:, 0]]
+    b = node_xy[face_nodes[:, 1]]
+    d = np.stack([b[:, 1] - a[:, 1], a[:, 0] - b[:, 0]], 1)
+    mid = 0.5 * (a + b)
+    flip = np.einsum("ij,ij->i", d, mid - c0_point) > 0
+    fn = face_nodes.copy()
+    fn[flip] = fn[flip][:, ::-1]
+    return fn
+
+
+def reorient(mesh, mode="fluent", seed=0):
+    """Copy of ``mesh`` with face node orders reversed: ``"fluent"`` reverses
+    every face (area vectors point out of c0, as in the shipped Fluent
+    meshes, which the reference's flag logic handles backwards), ``"random"``
+    reverses a random half of the faces."""
+    m = dict(mesh)
+    fn = mesh["face_nodes"].copy()
+    if mode == "fluent":
+        flip = np.ones(len(fn), bool)
+    else:
+        flip = np.random.default_rng(seed).random(len(fn)) < 0.5
+    fn[flip] = fn[flip][:, ::-1]
+    m["face_nodes"] = fn
+    return m
+
+
+def with_zone_types(mesh, old, new):
+    """Copy of ``mesh`` with zones of type ``old`` retyped to ``new``."""
+    m = dict(mesh)
+    z = mesh["zones"].copy()
+    z[z[:, 3] == old, 3] = new
+    m["zones"] = z
+    return m
+
+
+def sod_strip(nx=1000, ny=4, length=1.0, height=0.01, ends=OUTLET):
+    """Quad strip [0,L]x[0,H] of nx*ny cells (Sod tube).  Zones: interior,
+    bottom and top walls (slip), left and right ends of type ``ends``."""
+    xs = np.linspace(0.0, length, nx + 1)
+    ys = np.linspace(0.0, height, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    node_xy = np.stack([X.ravel(), Y.ravel()], 1)
+    nid = lambda i, j: i * (ny + 1) + j
+    cid = lambda i, j: i * ny + j
+    faces, cells, kinds = [], [], []
+    # interior vertical faces x = x_i, between cells (i-1, j) and (i, j)
+    I, J = np.meshgrid(np.arange(1, nx), np.arange(ny), indexing="ij")
+    I, J = I.ravel(), J.ravel()
+    faces.append(np.stack([nid(I, J + 1), nid(I, J)], 1))
+    cells.append(np.stack([cid(I - 1, J), cid(I, J)], 1))
+    # interior horizontal faces y = y_j, between (i, j-1) and (i, j)
+    I, J = np.meshgrid(np.arange(nx), np.arange(1, ny), indexing="ij")
+    I, J = I.ravel(), J.ravel()
+    faces.append(np.stack([nid(I, J), nid(I + 1, J)], 1))
+    cells.append(np.stack([cid(I, J - 1), cid(I, J)], 1))
+    n_int = sum(len(f) for f in faces)
+    bnd = []
+    i = np.arange(nx)
+    bnd.append((np.stack([nid(i + 1, 0), nid(i, 0)], 1), cid(i, 0), WALL))
+    bnd.append((np.stack([nid(i, ny), nid(i + 1, ny)], 1), cid(i, ny - 1), WALL))
+    j = np.arange(ny)
+    bnd.append((np.stack([nid(0, j), nid(0, j + 1)], 1), cid(0, j), ends))
+    bnd.append((np.stack([nid(nx, j + 1), nid(nx, j)], 1), cid(nx - 1, j), ends))
+    zones = [(1, 1, n_int, INTERIOR)]
+    start = n_int + 1
+    for k, (fn, c0, ty) in enumerate(bnd):
+        faces.append(fn)
+        cells.append(np.stack([c0, -np.ones_like(c0)], 1))
+        zones.append((2 + k, start, start + len(fn) - 1, ty))
+        start += len(fn)
+    face_nodes = np.concatenate(faces).astype(np.int32)
+    face_cells = np.concatenate(cells).astype(np.int32)
+    # cell centroids for the orientation check
+    cc = np.zeros((nx * ny, 2))
+    II, JJ = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    cc[cid(II, JJ).ravel()] = np.stack(
+        [0.5 * (xs[II] + xs[II + 1]).ravel(), 0.5 * (ys[JJ] + ys[JJ + 1]).ravel()], 1)
+    face_nodes = _orient_into_c0(node_xy, face_nodes, face_cells, cc[face_cells[:, 0]])
+    return dict(node_xy=node_xy, face_nodes=face_nodes, face_cells=face_cells,
+                zones=np.array(zones, np.int32), n_cells=nx * ny)
+
+
+def _edges_from_tris(tri_nodes, tri_xy):
+    """Unique edges of a triangulation given per-triangle node ids."""
+    e = np.concatenate([tri_nodes[:, [0, 1]], tri_nodes[:, [1, 2]], tri_nodes[:, [2, 0]]])
+    owner = np.tile(np.arange(len(tri_nodes)), 3)
+    key = np.sort(e, 1)
+    return e, owner, key
+
+
+def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
+            left=INLET, right=OUTLET, bottom=WALL, top=SYMMETRY):
+    """Jittered Delaunay triangles on a box, one boundary zone per side."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    hx, hy = lx / nx, ly / ny
+    X, Y = np.meshgrid(np.linspace(0, lx, nx + 1), np.linspace(0, ly, ny + 1), indexing="ij")
+    jx = rng.uniform(-jitter, jitter, X.shape) * hx
+    jy = rng.uniform(-jitter, jitter, Y.shape) * hy
+    jx[0, :] = jx[-1, :] = 0
+    jy[:, 0] = jy[:, -1] = 0
+    pts = np.stack([(X + jx).ravel(), (Y + jy).ravel()], 1)
+    tri = Delaunay(pts).simplices.astype(np.int64)
+    a, b, c = pts[tri[:, 0]], pts[tri[:, 1]], pts[tri[:, 2]]
+    area = 0.5 * ((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
+    tri = tri[np.abs(area) > 1e-14 * hx * hy]
+    cen = pts[tri].mean(1)
+    e, owner, key = _edges_from_tris(tri, pts)
+    k = key[:, 0] * len(pts) + key[:, 1]
+    order = np.argsort(k, kind="stable")
+    ks = k[order]
+    first = np.ones(len(ks), bool)
+    first[1:] = ks[1:] != ks[:-1]
+    grp = np.cumsum(first) - 1
+    n_e = grp[-1] + 1
+    c0 = np.full(n_e, -1)
+    c1 = np.full(n_e, -1)
+    en = np.zeros((n_e, 2), np.int64)
+    idx_first = order[first]
+    c0[:] = owner[idx_first]
+    en[:] = e[idx_first]
+    second = ~first
+    c1[grp[second]] = owner[order[second]]
+    interior = c1 >= 0
+    mid = pts[en].mean(1)
+    tol = 1e-9
+    side = np.full(n_e, -1)
+    side[~interior & (np.abs(mid[:, 0]) < tol * lx)] = 0
+    side[~interior & (np.abs(mid[:, 0] - lx) < tol * lx)] = 1
+    side[~interior & (np.abs(mid[:, 1]) < tol * ly)] = 2
+    side[~interior & (np.abs(mid[:, 1] - ly) < tol * ly)] = 3
+    if np.any(~interior & (side < 0)):
+        raise RuntimeError("boundary edge off the box")
+    kinds = [left, right, bottom, top]
+    sel = [np.where(interior)[0]] + [np.where(side == s)[0] for s in range(4)]
+    faces = np.concatenate([en[s] for s in sel]).astype(np.int32)
+    fc = np.stack([np.concatenate([c0[s] for s in sel]),
+                   np.concatenate([c1[s] for s in sel])], 1).astype(np.int32)
+    zones, start = [], 1
+    for zi, (s, ty) in enumerate(zip(sel, [INTERIOR] + kinds)):
+        zones.append((zi + 1, start, start + len(s) - 1, ty))
+        start += len(s)
+    zones = [z for z in zones if z[2] >= z[1]]
+    fn = _orient_into_c0(pts, faces, fc, cen[fc[:, 0]])
+    return dict(node_xy=pts, face_nodes=fn, face_cells=fc,
+                zones=np.array(zones, np.int32), n_cells=len(tri))
+
+
+def periodic_delaunay(n=1000, length=10.0, jitter=0.25, seed=20261203):
+    """Jittered Delaunay triangulation of the periodic square [0,L)^2.
+
+    Nodes: an n x n lattice with spacing h = L/n, each node moved by
+    U(-jitter*h, +jitter*h) per axis from ``numpy.random.default_rng(seed)``.
+    The Delaunay triangulation of the lattice plus a periodic ghost layer is
+    computed with scipy (Qhull); triangles whose centroid lies in [0,L)^2
+    form the mesh.  Every edge becomes one interior face; faces that cross
+    the periodic boundary carry c1_shift, the translation that maps cell
+    c1's coordinates into the frame of the face (and of c0).  Node
+    coordinates are stored per face frame (ghost images are separate nodes).
+    """
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    h = length / n
+    I, J = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    base = np.stack([I.ravel() * h, J.ravel() * h], 1)
+    base = base + rng.uniform(-jitter * h, jitter * h, base.shape)
+    # ghost layer of width g nodes on every side
+    g = 3
+    oi, oj = np.meshgrid(np.arange(-g, n + g), np.arange(-g, n + g), indexing="ij")
+    bi, bj = oi % n, oj % n
+    sx, sy = (oi - bi) // n, (oj - bj) // n
+    src = (bi * n + bj).ravel()
+    shift = np.stack([sx.ravel(), sy.ravel()], 1)
+    pts = base[src] + shift * length
+    tri = Delaunay(pts).simplices.astype(np.int64)
+    cen = pts[tri].mean(1)
+    inside = np.all((cen >= 0) & (cen < length), 1)
+    kept = tri[inside]
+    nT = len(kept)
+    # edges of the kept triangles, each in its triangle's own frame
+    e_pts = np.concatenate([kept[:, [0, 1]], kept[:, [1, 2]], kept[:, [2, 0]]])
+    owner = np.tile(np.arange(nT), 3)
+    # canonical key of an edge: its base node ids and the periodic offset
+    # between its endpoints' frames (the same on both sides of the edge)
+    ea, eb = e_pts[:, 0], e_pts[:, 1]
+    sa, sb = src[ea], src[eb]
+    da, db = shift[ea], shift[eb]
+    # orient the key so that the smaller base id comes first
+    swap = sa > sb
+    k0 = np.where(swap, sb, sa)
+    k1 = np.where(swap, sa, sb)
+    rel = np.where(swap[:, None], da - db, db - da).astype(np.int64)  # offset of k1 rel. k0
+    ekey = ((k0 * (n * n) + k1) * 3 + (rel[:, 0] + 1)) * 3 + (rel[:, 1] + 1)
+    eo = np.argsort(ekey, kind="stable")
+    eks = ekey[eo]
+    first = np.ones(len(eks), bool)
+    first[1:] = eks[1:] != eks[:-1]
+    if not np.all(first[::2]) or np.any(first[1::2]):
+        raise RuntimeError("periodic triangulation is not a closed torus")
+    i0 = eo[0::2]
+    i1 = eo[1::2]
+    c0 = owner[i0]
+    c1 = owner[i1]
+    # c1_shift: translation mapping c1's frame onto the edge as seen by c0
+    pa0 = pts[ea[i0]]
+    # endpoint of i1 with the same base id as endpoint a of i0
+    same = src[ea[i1]] == src[ea[i0]]
+    pa1 = np.where(same[:, None], pts[ea[i1]], pts[eb[i1]])
+    c1_shift = pa0 - pa1
+    c1_shift = np.round(c1_shift / length) * length
+    # frame of each triangle is the positions of its own vertices; nodes per
+    # face are the c0-frame positions, deduplicated
+    fa = pts[ea[i0]]
+    fb = pts[eb[i0]]
+    allp = np.concatenate([fa, fb])
+    q = np.round(allp / (h * 1e-6)).astype(np.int64)
+    _, uidx, inv = np.unique(q[:, 0] * (1 << 31) + q[:, 1], return_index=True,
+                             return_inverse=True)
+    node_xy = allp[uidx]
+    nf = len(i0)
+    face_nodes = np.stack([inv[:nf], inv[nf:]], 1).astype(np.int32)
+    face_cells = np.stack([c0, c1], 1).astype(np.int32)
+    cen_k = pts[kept].mean(1)
+    face_nodes = _orient_into_c0(node_xy, face_nodes, face_cells, cen_k[c0])
+    zones = np.array([(1, 1, nf, INTERIOR)], np.int32)
+    return dict(node_xy=node_xy, face_nodes=face_nodes, face_cells=face_cells,
+                zones=zones, n_cells=nT, c1_shift=c1_shift, cell_centroid=cen_k)
+
+
+def write_msh(path, mesh, crlf=False):
+    """Fluent ASCII 2D .msh of the subset the reference reader parses
+    (lower-case hex ids, single spaces, interior zone first)."""
+    nl = "\r\n" if crlf else "\n"
+    xy, fn, fc, zones = mesh["node_xy"], mesh["face_nodes"], mesh["face_cells"], mesh["zones"]
+    nN, nF, nC = len(xy), len(fn), int(mesh["n_cells"])
+    out = ['(0 "mstcfd meshgen")', "(2 2)",
+           f"(10 (0 1 {nN:x} 0 2))", f"(10 (1 1 {nN:x} 1 2)", "("]
+    out += [f"{x!r} {y!r}" for x, y in xy.tolist()]
+    out += ["))", f"(12 (0 1 {nC:x} 0 0))", f"(12 (2 1 {nC:x} 1 1))",
+            f"(13 (0 1 {nF:x} 0 0))"]
+    for zi, (zid, st, en, ty) in enumerate(zones.tolist()):
+        out.append(f'(0 "zone {zi}")')
+        out.append(f"(13 ({zid + 2:x} {st:x} {en:x} {ty:x} 2)(")
+        for f in range(st - 1, en):
+            a, b = fn[f] + 1
+            c0, c1 = fc[f] + 1
+            out.append(f"{a:x} {b:x} {c0:x} {c1 if c1 > 0 else 0:x}")
+        out.append("))")
+    with open(path, "w", newline="") as fh:
+        fh.write(nl.join(out) + nl)
+
+
+# ---------------------------------------------------------------------------
+# initial states
+# ---------------------------------------------------------------------------
+def reference_inlet():
+    """CONST.h:70-83 as the macros expand: (1, 0, 0, 1/286.32*715.8)."""
+    return np.array([1.0, 1.0 * 0, 1.0 * 0, 1 * (1 / 286.32 * 715.8 + 0.5 * (0 * 0 + 0 * 0))])
+
+
+def sod_state(cell_ctr, x0=0.5):
+    """Time::initialization (time/Time.cpp:13-53): the reference state, with
+    rho scaled by 0.125 and E by 0.1 where the cell centre x > x0."""
+    q = np.tile(reference_inlet(), (len(cell_ctr), 1))
+    right = cell_ctr[:, 0] > x0
+    q[right, 0] *= 0.125
+    q[right, 3] *= 0.1
+    return q
+
+
+def primitive_to_q(rho, u, v, p):
+    return np.stack([rho, rho * u, rho * v, p / (GAMMA - 1) + 0.5 * rho * (u * u + v * v)], -1)
+
+
+def q_to_primitive(q):
+    rho = q[..., 0]
+    u, v = q[..., 1] / rho, q[..., 2] / rho
+    p = (GAMMA - 1) * (q[..., 3] - 0.5 * rho * (u * u + v * v))
+    return rho, u, v, p
+
+
+def isentropic_vortex(xy, t=0.0, length=10.0, beta=5.0, mach=0.5, x0=None):
+    """Isentropic vortex of strength beta convected along +x at the given
+    Mach number (free stream rho = p = 1) on the periodic square [0,L)^2,
+    as the sum over the nearest periodic images."""
+    x0 = np.array([length / 2, length / 2]) if x0 is None else np.asarray(x0)
+    ainf = np.sqrt(GAMMA)
+    uinf = mach * ainf
+    c = x0 + np.array([uinf * t, 0.0])
+    du = np.zeros(len(xy))
+    dv = np.zeros(len(xy))
+    dT = np.zeros(len(xy))
+    for ix in (-1, 0, 1):
+        for iy in (-1, 0, 1):
+            cx = (c[0] % length) + ix * length
+            cy = (c[1] % length) + iy * length
+            dx, dy = xy[:, 0] - cx, xy[:, 1] - cy
+            r2 = dx * dx + dy * dy
+            e = np.exp(0.5 * (1 - r2))
+            du += -beta / (2 * np.pi) * dy * e
+            dv += beta / (2 * np.pi) * dx * e
+            dT += -(GAMMA - 1) * beta ** 2 / (8 * GAMMA * np.pi ** 2) * e * e
+    T = 1.0 + dT
+    rho = T ** (1 / (GAMMA - 1))
+    p = rho * T
+    return primitive_to_q(rho, uinf + du, dv, p)
+
+
+def random_state(n, seed=0, umax=2.0):
+    """Random physical states: rho, p in [0.5, 1.5], |u|,|v| <= umax."""
+    r = np.random.default_rng(seed)
+    return primitive_to_q(r.uniform(0.5, 1.5, n), r.uniform(-umax, umax, n),
+                          r.uniform(-umax, umax, n), r.uniform(0.5, 1.5, n))
+
+
+def smooth_state(xy, amp=0.2, umax=0.8):
+    """Smooth, physical, non-uniform state (for 2nd-order parity cases)."""
+    x, y = xy[:, 0], xy[:, 1]
+    rho = 1 + amp * np.sin(3.1 * x + 0.7) * np.cos(2.3 * y + 0.2)
+    u = umax * np.cos(1.7 * x - 0.4) * np.sin(2.9 * y + 1.1)
+    v = umax * np.sin(2.2 * x + 0.3) * np.cos(1.3 * y - 0.5)
+    p = 1 + amp * np.cos(2.7 * x - 1.0) * np.sin(1.9 * y + 0.4)
+    return primitive_to_q(rho, u, v, p)
