@@ -164,8 +164,9 @@ mst_status mst_solve(mst_ctx *c);
 /* RhoSolver::updateNewToOld (RhoSolver.cpp:513-517). */
 mst_status mst_update_new_to_old(mst_ctx *c);
 
-/* Per-cell residual R of the last solve(), [n_cells][4] (the reference's
- * integralConvectFlux, RhoSolver.cpp:47-56). */
+/* Per-cell residual R of the last mst_solve(), [n_cells][4] (the
+ * reference's integralConvectFlux, RhoSolver.cpp:47-56).  mst_step does not
+ * store it. */
 mst_status mst_get_residual(mst_ctx *c, double *r, size_t stride);
 /* Per-face flux matrices of the last solve(), [n_faces][2][4]
  * (p1OldFaceConvectFlux, RhoSolver.cpp:90-369). */
@@ -196,6 +197,26 @@ mst_status mst_get_time(mst_ctx *c, double *t);
  * context's stream: elapsed milliseconds between its first and last
  * kernel, and the number of kernels launched. */
 mst_status mst_last_timing(mst_ctx *c, double *ms, int *launches);
+
+/* Per-kernel CUDA-event timing on the context's stream.  When enabled,
+ * every kernel launch of mst_solve/mst_step is bracketed by events; the
+ * totals accumulate until mst_profile_reset. */
+mst_status mst_profile_enable(mst_ctx *c, int on);
+mst_status mst_profile_reset(mst_ctx *c);
+/* Number of distinct kernels timed so far. */
+int mst_profile_count(mst_ctx *c);
+/* Stats of kernel i: its name (copied into name, NUL-terminated), number
+ * of launches and total device milliseconds. */
+mst_status mst_profile_get(mst_ctx *c, int i, char *name, size_t name_len,
+                           int *launches, double *total_ms);
+
+/* Page-locked host buffers for fast host<->device copies of states
+ * (cudaHostAlloc / cudaFreeHost). */
+mst_status mst_host_alloc(size_t bytes, void **out);
+mst_status mst_host_free(void *p);
+
+/* Number of CUDA devices visible to this process. */
+mst_status mst_device_count(int *n);
 
 /* Text of the last error on this thread (static storage). */
 const char *mst_last_error(void);

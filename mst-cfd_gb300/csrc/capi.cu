@@ -154,6 +154,14 @@ struct mst_ctx {
   double* scal = nullptr;      // [0] dt, [1] time
   double* norms = nullptr;     // [kNormSlots + 2]
   int last_launches = 0;
+  // per-kernel event timing
+  bool profiling = false;
+  struct Pending { int kernel; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::string> kname;
+  std::vector<int> klaunch;
+  std::vector<double> kms;
   bool timed = false;
   bool grad_valid = false;
   std::vector<void*> allocs;
@@ -183,7 +191,63 @@ mst_status check_params(const mst_params* p) {
   return MST_OK;
 }
 
+cudaEvent_t take_event(mst_ctx* c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+int kernel_index(mst_ctx* c, const char* name) {
+  for (size_t i = 0; i < c->kname.size(); ++i)
+    if (c->kname[i] == name) return (int)i;
+  c->kname.push_back(name);
+  c->klaunch.push_back(0);
+  c->kms.push_back(0.0);
+  return (int)c->kname.size() - 1;
+}
+
+// brackets one launch with events when profiling is on
+struct ProfScope {
+  mst_ctx* c;
+  int k = -1;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(mst_ctx* ctx, const char* name) : c(ctx) {
+    if (!c->profiling) return;
+    k = kernel_index(c, name);
+    a = take_event(c);
+    b = take_event(c);
+    cudaEventRecord(a, c->stream);
+  }
+  ~ProfScope() {
+    if (k < 0) return;
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({k, a, b});
+  }
+};
+
+// folds the finished launches into the per-kernel totals
+void drain_profile(mst_ctx* c) {
+  if (c->pending.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& p : c->pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      c->klaunch[p.kernel] += 1;
+      c->kms[p.kernel] += ms;
+    }
+    c->event_pool.push_back(p.a);
+    c->event_pool.push_back(p.b);
+  }
+  c->pending.clear();
+}
+
 mst_status launch_grad(mst_ctx* c, const double4_32a* q) {
+  ProfScope ps(c, c->p.precision == MST_PREC_FP32 ? "k_gradient<f32>" : "k_gradient<f64>");
   cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                       ? mst::exact::launch_gradient(prec_of(c->p), c->dm, q, c->grad,
                                                     c->p.reference_quirks, c->stream)
@@ -196,6 +260,7 @@ mst_status launch_grad(mst_ctx* c, const double4_32a* q) {
 }
 
 mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
+  ProfScope ps(c, c->p.precision == MST_PREC_FP32 ? "k_flux_update<f32>" : "k_flux_update<f64>");
   cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                       ? mst::exact::launch_flux_update(prec_of(c->p), c->p.flux, c->p.order,
                                                        c->dm, a, 0, c->stream)
@@ -218,7 +283,8 @@ mst::StepArgs base_args(mst_ctx* c) {
 
 // one residual evaluation + update of stage 'stage' from q into qn
 mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
-                     double4_32a* qn, int stage, bool fixed_dt, bool norms) {
+                     double4_32a* qn, int stage, bool fixed_dt, bool norms,
+                     bool keep_residual) {
   if (c->p.order == 2) {
     mst_status s = launch_grad(c, q);
     if (s) return s;
@@ -227,7 +293,7 @@ mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
   a.q = q;
   a.q0 = q0;
   a.qn = qn;
-  a.r_out = c->r;
+  a.r_out = keep_residual ? c->r : nullptr;
   a.stage = stage;
   if (!fixed_dt) {
     if (c->p.dt_mode == MST_DT_CFL_LOCAL) a.dt_cell = c->dt_cell;
@@ -241,6 +307,7 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end) {
   const int nC = c->dm.n_cells;
   int mode = 0;
   if (c->p.dt_mode != MST_DT_FIXED) {
+    ProfScope ps(c, "k_spectral_dt");
     cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                         ? mst::exact::launch_spectral_dt(prec_of(c->p), c->dm, q, c->p.cfl,
                                                          c->dt_cell, c->dt_part, c->stream)
@@ -250,6 +317,7 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end) {
     if (e != cudaSuccess) return fail(MST_ECUDA, std::string("spectral_dt: ") + cudaGetErrorString(e));
     mode = 1;
   }
+  ProfScope ps(c, "k_finalize_dt");
   k_finalize_dt<<<1, 1024, 0, c->stream>>>(c->dt_part, (nC + 255) / 256, mode, c->p.dt,
                                             t_end, c->scal);
   c->last_launches++;
@@ -258,6 +326,7 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end) {
 }
 
 mst_status finalize_norms(mst_ctx* c, bool advance) {
+  ProfScope ps(c, "k_finalize_norms");
   k_finalize_norms<<<1, dim3(64, kNormSlots), 0, c->stream>>>(
       c->partials, c->dm.n_tiles, c->dm.n_cells, advance ? 1 : 0, c->scal, c->norms);
   c->last_launches++;
@@ -523,6 +592,11 @@ mst_status mst_ctx_destroy(mst_ctx* c) {
   if (!c) return MST_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
+  for (auto& p : c->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -584,12 +658,13 @@ mst_status mst_solve(mst_ctx* c) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   c->last_launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
-  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true);
+  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true, true);
   if (s) return s;
   if ((s = finalize_norms(c, false))) return s;
   CU(cudaEventRecord(c->ev1, c->stream));
   c->timed = true;
   CU(cudaStreamSynchronize(c->stream));
+  drain_profile(c);
   return MST_OK;
 }
 
@@ -667,10 +742,10 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
     mst_status st = compute_dt(c, c->q_old, t_end);
     if (st) return st;
     if (c->p.time_scheme == MST_TIME_EULER) {
-      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, true);
+      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, true, false);
     } else {
-      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false);
-      if (!st) st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, true);
+      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false, false);
+      if (!st) st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, true, false);
     }
     if (st) return st;
     if ((st = finalize_norms(c, true))) return st;
@@ -679,8 +754,68 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
   CU(cudaEventRecord(c->ev1, c->stream));
   c->timed = true;
   c->grad_valid = false;
+  drain_profile(c);
   if (last) return read_norms(c, last);
   CU(cudaStreamSynchronize(c->stream));
+  return MST_OK;
+}
+
+mst_status mst_profile_enable(mst_ctx* c, int on) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  drain_profile(c);
+  c->profiling = on != 0;
+  return MST_OK;
+}
+
+mst_status mst_profile_reset(mst_ctx* c) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  drain_profile(c);
+  c->kname.clear();
+  c->klaunch.clear();
+  c->kms.clear();
+  return MST_OK;
+}
+
+int mst_profile_count(mst_ctx* c) {
+  if (!c) return 0;
+  drain_profile(c);
+  return (int)c->kname.size();
+}
+
+mst_status mst_profile_get(mst_ctx* c, int i, char* name, size_t name_len,
+                           int* launches, double* total_ms) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  drain_profile(c);
+  if (i < 0 || i >= (int)c->kname.size()) return fail(MST_EINVAL, "no such kernel");
+  if (name && name_len) {
+    std::strncpy(name, c->kname[i].c_str(), name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (launches) *launches = c->klaunch[i];
+  if (total_ms) *total_ms = c->kms[i];
+  return MST_OK;
+}
+
+mst_status mst_host_alloc(size_t bytes, void** out) {
+  if (!out) return fail(MST_EINVAL, "NULL argument");
+  *out = nullptr;
+  CU(cudaHostAlloc(out, std::max<size_t>(bytes, 1), cudaHostAllocDefault));
+  return MST_OK;
+}
+
+mst_status mst_host_free(void* p) {
+  if (p) CU(cudaFreeHost(p));
+  return MST_OK;
+}
+
+mst_status mst_device_count(int* n) {
+  if (!n) return fail(MST_EINVAL, "NULL argument");
+  *n = 0;
+  cudaError_t e = cudaGetDeviceCount(n);
+  if (e != cudaSuccess) {
+    *n = 0;
+    return fail(MST_ECUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+  }
   return MST_OK;
 }
 

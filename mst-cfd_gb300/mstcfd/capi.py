@@ -108,6 +108,14 @@ def load():
         "mst_step": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(Norms)]),
         "mst_get_time": (C.c_int, [C.c_void_p, _dp]),
         "mst_last_timing": (C.c_int, [C.c_void_p, _dp, _ip]),
+        "mst_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
+        "mst_profile_reset": (C.c_int, [C.c_void_p]),
+        "mst_profile_count": (C.c_int, [C.c_void_p]),
+        "mst_profile_get": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t,
+                                      _ip, _dp]),
+        "mst_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+        "mst_host_free": (C.c_int, [C.c_void_p]),
+        "mst_device_count": (C.c_int, [_ip]),
         "mst_last_error": (C.c_char_p, []),
         "mst_abi_version": (C.c_int, []),
     }

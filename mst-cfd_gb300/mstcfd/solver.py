@@ -164,6 +164,30 @@ class Solver:
         capi.check(capi.load().mst_last_timing(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def profile(self, on=True):
+        capi.check(capi.load().mst_profile_enable(self._h, int(on)))
+
+    def profile_reset(self):
+        capi.check(capi.load().mst_profile_reset(self._h))
+
+    def profile_stats(self):
+        """{kernel name: (launches, total ms)} of the profiled launches."""
+        L = capi.load()
+        out = {}
+        buf = C.create_string_buffer(128)
+        for i in range(L.mst_profile_count(self._h)):
+            n, ms = C.c_int(), C.c_double()
+            capi.check(L.mst_profile_get(self._h, i, buf, 128, C.byref(n), C.byref(ms)))
+            out[buf.value.decode()] = (n.value, ms.value)
+        return out
+
+    def set_state_ptr(self, ptr, stride=4):
+        """State in from a raw host pointer (e.g. a pinned buffer)."""
+        capi.check(capi.load().mst_set_state(self._h, C.cast(ptr, capi._dp), stride))
+
+    def get_state_ptr(self, ptr, stride=4):
+        capi.check(capi.load().mst_get_state(self._h, C.cast(ptr, capi._dp), stride))
+
     def close(self):
         h = getattr(self, "_h", None)
         if h:
@@ -213,3 +237,26 @@ class RhoSolver:
 
     def residual(self):
         return self._s.residual()
+
+
+class PinnedArray:
+    """A page-locked host array (mst_host_alloc) viewed through numpy."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = C.c_void_p()
+        capi.check(capi.load().mst_host_alloc(self.nbytes, C.byref(self.ptr)))
+        buf = (C.c_char * self.nbytes).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            capi.load().mst_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -444,6 +444,16 @@ int om_mesh_from_arrays(int n_nodes, const double *node_xy, int n_cells,
                         int n_faces, const int *face_nodes,
                         const int *face_cells, int n_zones, const int *zones,
                         om_mesh **out) {
+  return om_mesh_from_arrays_periodic(n_nodes, node_xy, n_cells, n_faces,
+                                      face_nodes, face_cells, n_zones, zones,
+                                      NULL, out);
+}
+
+int om_mesh_from_arrays_periodic(int n_nodes, const double *node_xy,
+                                 int n_cells, int n_faces,
+                                 const int *face_nodes, const int *face_cells,
+                                 int n_zones, const int *zones,
+                                 const double *c1_shift, om_mesh **out) {
   *out = NULL;
   if (n_nodes <= 0 || n_cells <= 0 || n_faces <= 0 || n_zones <= 0)
     return OM_EINVAL;
@@ -452,6 +462,10 @@ int om_mesh_from_arrays(int n_nodes, const double *node_xy, int n_cells,
   memcpy(m->face_nodes, face_nodes, sizeof(int) * 2 * n_faces);
   memcpy(m->face_cells, face_cells, sizeof(int) * 2 * n_faces);
   m->n_zones = n_zones;
+  if (c1_shift) {
+    m->face_shift = (double *)xcalloc((size_t)2 * n_faces, 8);
+    memcpy(m->face_shift, c1_shift, sizeof(double) * 2 * n_faces);
+  }
   m->zone = (int *)xcalloc((size_t)4 * n_zones, 4);
   memcpy(m->zone, zones, sizeof(int) * 4 * n_zones);
   m->n_int_faces = 0;
@@ -499,10 +513,23 @@ void om_mesh_free(om_mesh *m) {
   free(m->inner);
   free(m->bond1);
   free(m->bond2);
+  free(m->face_shift);
   free(m);
 }
 
 static double norm2(double a, double b) { return sqrt(a * a + b * b); }
+
+/* shift of face f's c1 image (zero without periodic images) */
+static double shift_of(const om_mesh *m, int f, int d) {
+  return m->face_shift ? m->face_shift[2 * f + d] : 0.0;
+}
+/* centre of face f as seen from cell c: the c1 side of a periodic face
+ * sees it translated back into its own frame */
+static double face_ctr_from(const om_mesh *m, int f, int c, int d) {
+  double x = m->face_ctr[2 * f + d];
+  if (m->face_shift && m->face_cells[2 * f] != c) x = x - m->face_shift[2 * f + d];
+  return x;
+}
 
 /* Geometry and derived connectivity: MshBlock.cpp:238-259 (cell lists),
  * Face::setCenter (Face.cpp:8-19), Cell::setCenter/setVolume
@@ -566,12 +593,12 @@ static int geometry(om_mesh *m) {
     int b = m->cell_ptr[c], n = m->cell_ptr[c + 1] - b;
     for (int d = 0; d < 2; ++d) {
       double s = 0.0;
-      for (int k = 0; k < n; ++k) s += m->face_ctr[2 * m->cell_faces[b + k] + d];
+      for (int k = 0; k < n; ++k) s += face_ctr_from(m, m->cell_faces[b + k], c, d);
       m->cell_ctr[2 * c + d] = s / (double)n;
     }
 #define LEN(k) norm2(m->face_dir[2 * m->cell_faces[b + (k)]], \
                      m->face_dir[2 * m->cell_faces[b + (k)] + 1])
-#define FC(k, d) m->face_ctr[2 * m->cell_faces[b + (k)] + (d)]
+#define FC(k, d) face_ctr_from(m, m->cell_faces[b + (k)], c, (d))
     double vol = 0.0;
     if (n == 3) {
       double l0 = LEN(0), l1 = LEN(1), l2 = LEN(2);
@@ -629,10 +656,11 @@ static int geometry(om_mesh *m) {
     int c0 = m->face_cells[2 * i], c1 = m->face_cells[2 * i + 1];
     if (c1 >= 0) {
       const double *fc = m->face_ctr + 2 * i;
-      double n1 = norm2(m->cell_ctr[2 * c1] - fc[0], m->cell_ctr[2 * c1 + 1] - fc[1]);
+      double x1 = m->cell_ctr[2 * c1] + shift_of(m, i, 0);
+      double y1 = m->cell_ctr[2 * c1 + 1] + shift_of(m, i, 1);
+      double n1 = norm2(x1 - fc[0], y1 - fc[1]);
       double n0 = norm2(m->cell_ctr[2 * c0] - fc[0], m->cell_ctr[2 * c0 + 1] - fc[1]);
-      double n1b = norm2(m->cell_ctr[2 * c1] - fc[0], m->cell_ctr[2 * c1 + 1] - fc[1]);
-      m->face_eta0[i] = n1 / (n0 + n1b);
+      m->face_eta0[i] = n1 / (n0 + n1);
     } else {
       m->face_eta0[i] = 1;
     }

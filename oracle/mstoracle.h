@@ -51,6 +51,10 @@ typedef struct om_mesh {
   double *cell_ctr;    /* [n_cells][2] */
   double *cell_vol;    /* [n_cells] */
   int *inner, *bond1, *bond2;
+  /* periodic images (project extension; NULL for reference meshes):
+   * [n_faces][2] translation mapping cell c1's coordinates into the frame
+   * of the face and of c0 */
+  double *face_shift;
 } om_mesh;
 
 /* status codes (match the product's C ABI) */
@@ -66,6 +70,12 @@ int om_mesh_from_arrays(int n_nodes, const double *node_xy, int n_cells,
                         int n_faces, const int *face_nodes,
                         const int *face_cells, int n_zones, const int *zones,
                         om_mesh **out);
+/* Same, with periodic image shifts (may be NULL). */
+int om_mesh_from_arrays_periodic(int n_nodes, const double *node_xy,
+                                 int n_cells, int n_faces,
+                                 const int *face_nodes, const int *face_cells,
+                                 int n_zones, const int *zones,
+                                 const double *c1_shift, om_mesh **out);
 void om_mesh_free(om_mesh *m);
 
 /* Flux schemes */
@@ -108,6 +118,48 @@ void om_solve(const om_mesh *m, const om_params *p, const double *q,
  * component, signed division as in time/Time.cpp:69-76. */
 void om_linf_change(int n_cells, const double *qold, const double *qnew,
                     double res[4]);
+
+/* ------------------------------------------------------------------ */
+/* Project extensions with no reference counterpart (mstoracle_ext.c):  */
+/* corrected boundary handling, TVD limiters, periodic images, CFL time */
+/* steps and the two-stage Runge-Kutta update.  Each restates the       */
+/* published method named at its definition, in the operation order of  */
+/* the CUDA kernels (so the FP64-exact GPU path matches bit-for-bit).   */
+/* ------------------------------------------------------------------ */
+#define OM_LIM_NONE 0
+#define OM_LIM_MINMOD 1
+#define OM_LIM_VANLEER 2
+#define OM_LIM_VANALBADA 3
+#define OM_DT_FIXED 0
+#define OM_DT_CFL_GLOBAL 1
+#define OM_DT_CFL_LOCAL 2
+
+typedef struct om_params_ext {
+  int flux, order, limiter;
+  int quirks;       /* 1: the reference's behaviour; 0: corrected */
+  int rk2;          /* 0 forward Euler, 1 two-stage SSP Runge-Kutta */
+  int dt_mode;      /* OM_DT_* */
+  double dt, cfl;
+  double inlet_q[4];
+} om_params_ext;
+
+typedef struct om_norms {
+  double linf[4], l2[4], mass, dt, time;
+} om_norms;
+
+void om_default_params_ext(om_params_ext *p);
+void om_gradient_ext(const om_mesh *m, const double *q, int quirks,
+                     double *grad);
+void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
+                      const double *q, const double *grad, double *F);
+/* per-cell CFL step dt_c = cfl V / (0.5 sum_f (|u.n| + a|n|)); returns
+ * the minimum (0 where the state is not physical) */
+double om_spectral_dt(const om_mesh *m, const double *q, double cfl,
+                      double *dt_cell);
+/* nsteps time steps in place; *time is advanced; last = norms of the last
+ * step (nullable) */
+int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
+                int nsteps, double t_end, double *time, om_norms *last);
 
 #ifdef __cplusplus
 }

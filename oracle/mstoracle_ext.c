@@ -1,0 +1,261 @@
+/* Oracle extensions beyond the reference (test infrastructure only; see
+ * mstoracle.h).  The reference has no limiter, no CFL or local time step,
+ * no Runge-Kutta update and no periodic faces, and its 2nd-order outlet
+ * and symmetry faces are broken (RhoSolver.cpp:320-361); these functions
+ * restate the methods the CUDA path implements for them, in the kernels'
+ * operation order.  Compile with -ffp-contract=off. */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "mstoracle.h"
+
+void om_default_params_ext(om_params_ext *p) {
+  memset(p, 0, sizeof *p);
+  p->flux = OM_AUSM;
+  p->order = 1;
+  p->quirks = 1;
+  p->dt = 1.0 / 4e+3;
+  p->cfl = 0.5;
+  om_reference_inlet(p->inlet_q);
+}
+
+static double shift(const om_mesh *m, int f, int d) {
+  return m->face_shift ? m->face_shift[2 * f + d] : 0.0;
+}
+
+/* Green-Gauss gradient of conserved Q from eta0-weighted face values
+ * (RhoSolver.cpp:430-453).  quirks = 1 copies c0 values from face nInt-1
+ * on (the reference's boundary loop); 0 from nInt. */
+void om_gradient_ext(const om_mesh *m, const double *q, int quirks,
+                     double *grad) {
+  const int first = quirks ? (m->n_int_faces > 0 ? m->n_int_faces - 1 : 0)
+                           : m->n_int_faces;
+  for (int c = 0; c < m->n_cells; ++c) {
+    double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = m->cell_ptr[c]; k < m->cell_ptr[c + 1]; ++k) {
+      const int f = m->cell_faces[k];
+      const int c0 = m->face_cells[2 * f], c1 = m->face_cells[2 * f + 1];
+      double fq[4];
+      if (f < first && c1 >= 0) {
+        const double e = m->face_eta0[f];
+        for (int j = 0; j < 4; ++j) fq[j] = e * q[4 * c0 + j] + (1 - e) * q[4 * c1 + j];
+      } else {
+        for (int j = 0; j < 4; ++j) fq[j] = q[4 * c0 + j];
+      }
+      for (int j = 0; j < 4; ++j) g[j] += fq[j] * m->cell_dof[2 * k];
+      for (int j = 0; j < 4; ++j) g[4 + j] += fq[j] * m->cell_dof[2 * k + 1];
+    }
+    for (int j = 0; j < 8; ++j) grad[8 * c + j] = g[j] / m->cell_vol[c];
+  }
+}
+
+static void mirror_e(double dx, double dy, const double in[4], double out[4]) {
+  const double nrm = sqrt(dx * dx + dy * dy);
+  const double n0 = dx / nrm, n1 = dy / nrm;
+  double t = n0 * in[1];
+  t += n1 * in[2];
+  out[0] = in[0];
+  out[1] = in[1] - 2.0 * n0 * t;
+  out[2] = in[2] - 2.0 * n1 * t;
+  out[3] = in[3];
+}
+
+static void recon_e(const double q[4], const double *g, double rx, double ry,
+                    double out[4]) {
+  for (int k = 0; k < 4; ++k) {
+    double s = g[k] * rx;
+    s += g[4 + k] * ry;
+    out[k] = q[k] + s;
+  }
+}
+
+/* TVD slope limiters psi(a, b) of the upwind difference a and the central
+ * difference b: minmod; van Leer 2ab/(a+b); van Albada
+ * (a(b^2+e) + b(a^2+e)) / (a^2+b^2+2e), e = 1e-12 (van Albada, van Leer &
+ * Roberts 1982); zero unless a and b have the same sign. */
+static double slope_e(int lim, double a, double b) {
+  if (!(a * b > 0.0)) return 0.0;
+  if (lim == OM_LIM_MINMOD) return fabs(a) < fabs(b) ? a : b;
+  if (lim == OM_LIM_VANLEER) return 2.0 * a * b / (a + b);
+  const double e = 1e-12;
+  return (a * (b * b + e) + b * (a * a + e)) / (a * a + b * b + 2.0 * e);
+}
+
+/* Face flux matrices with the extended options.  quirks = 1 is identical to
+ * om_face_flux.  quirks = 0: left/right from the geometry (c0 is left along
+ * axis d when its outward normal points +d), 2nd-order symmetry faces
+ * mirror the reconstructed state, 2nd-order outlets use the reconstructed
+ * state on both sides.  With a limiter (quirks = 0), interior faces use the
+ * edge-based MUSCL reconstruction Q_L = Q_0 + psi(2 G_0.d - dQ, dQ)/2,
+ * Q_R = Q_1 - psi(2 G_1.d - dQ, dQ)/2 with d = x_1 - x_0 (periodic image)
+ * and dQ = Q_1 - Q_0, which reduces to 1D MUSCL on a uniform grid; boundary
+ * faces are first order. */
+void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
+                      const double *q, const double *grad, double *F) {
+  void (*fl)(const double *, const double *, int, double *) =
+      (p->flux == OM_ROE) ? om_roe_flux : om_ausm_flux;
+  const int second = (p->order == 2);
+  const int limited = second && !p->quirks && p->limiter != OM_LIM_NONE;
+  for (int z = 0; z < m->n_zones; ++z) {
+    const int type = m->zone[4 * z + 3];
+    for (int i = m->zone[4 * z + 1] - 1; i < m->zone[4 * z + 2]; ++i) {
+      double *Fi = F + 8 * i;
+      const int c0 = m->face_cells[2 * i], c1 = m->face_cells[2 * i + 1];
+      const double *dv = m->face_dir + 2 * i;
+      int flag[2];
+      for (int d = 0; d < 2; ++d)
+        flag[d] = p->quirks ? m->face_flag[2 * i + d] : (m->face_dac[i] * dv[d] >= 0);
+      if (type != 2 && type != 3 && type != 5 && type != 7 && type != 10) {
+        memset(Fi, 0, 8 * sizeof(double));
+        continue;
+      }
+      const double *q0 = q + 4 * c0;
+      double r0x = 0, r0y = 0;
+      if (second) {
+        r0x = m->face_ctr[2 * i] - m->cell_ctr[2 * c0];
+        r0y = m->face_ctr[2 * i + 1] - m->cell_ctr[2 * c0 + 1];
+      }
+      double L[4], R[4];
+      if (type == 2) {
+        const double *q1 = q + 4 * c1;
+        if (!second) {
+          memcpy(L, q0, 32);
+          memcpy(R, q1, 32);
+        } else {
+          const double r1x = (m->face_ctr[2 * i] - shift(m, i, 0)) - m->cell_ctr[2 * c1];
+          const double r1y = (m->face_ctr[2 * i + 1] - shift(m, i, 1)) - m->cell_ctr[2 * c1 + 1];
+          const double *g0 = grad + 8 * c0, *g1 = grad + 8 * c1;
+          if (!limited) {
+            recon_e(q0, g0, r0x, r0y, L);
+            recon_e(q1, g1, r1x, r1y, R);
+          } else {
+            const double dx = r0x - r1x, dy = r0y - r1y;
+            for (int k = 0; k < 4; ++k) {
+              const double dc = q1[k] - q0[k];
+              const double du0 = 2.0 * (g0[k] * dx + g0[4 + k] * dy) - dc;
+              const double du1 = 2.0 * (g1[k] * dx + g1[4 + k] * dy) - dc;
+              L[k] = q0[k] + 0.5 * slope_e(p->limiter, du0, dc);
+              R[k] = q1[k] - 0.5 * slope_e(p->limiter, du1, dc);
+            }
+          }
+        }
+      } else {
+        const int recon_side = second && !limited && !(type == 7 && p->quirks) &&
+                               !(type == 5 && p->quirks);
+        if (recon_side) recon_e(q0, grad + 8 * c0, r0x, r0y, L);
+        else memcpy(L, q0, 32);
+        if (type == 10) {
+          memcpy(R, p->inlet_q, 32);
+        } else if (type == 5) {
+          memcpy(R, L, 32);
+        } else if (type == 7 && second && p->quirks && !limited) {
+          double rc[4], mm[4];
+          recon_e(q0, grad + 8 * c0, r0x, r0y, rc);
+          mirror_e(dv[0], dv[1], q0, mm);
+          R[0] = rc[0];
+          R[1] = mm[1];
+          R[2] = mm[2];
+          R[3] = rc[3];
+        } else {
+          mirror_e(dv[0], dv[1], L, R);
+        }
+      }
+      for (int d = 0; d < 2; ++d) {
+        if (flag[d]) fl(L, R, d, Fi + 4 * d);
+        else fl(R, L, d, Fi + 4 * d);
+      }
+    }
+  }
+}
+
+double om_spectral_dt(const om_mesh *m, const double *q, double cfl,
+                      double *dt_cell) {
+  double dmin = 1e300;
+  for (int c = 0; c < m->n_cells; ++c) {
+    const double *qs = q + 4 * c;
+    const double u = qs[1] / qs[0], v = qs[2] / qs[0];
+    const double ke = 0.5 * (qs[1] * qs[1] + qs[2] * qs[2]) / qs[0];
+    const double pr = (qs[3] - ke) * (1.4 - 1);
+    const double snd = sqrt(1.4 * pr / qs[0]);
+    double lam = 0.0;
+    for (int k = m->cell_ptr[c]; k < m->cell_ptr[c + 1]; ++k) {
+      const double *dv = m->face_dir + 2 * m->cell_faces[k];
+      lam += fabs(u * dv[0] + v * dv[1]) + snd * sqrt(dv[0] * dv[0] + dv[1] * dv[1]);
+    }
+    double dtc = cfl * m->cell_vol[c] / (0.5 * lam);
+    if (!(dtc > 0)) dtc = 0.0;
+    if (dt_cell) dt_cell[c] = dtc;
+    if (dtc < dmin) dmin = dtc;
+  }
+  return dmin;
+}
+
+/* residual R(q) of every cell with the extended options */
+static void residual_ext(const om_mesh *m, const om_params_ext *p,
+                         const double *q, double *F, double *grad, double *R) {
+  if (p->order == 2) om_gradient_ext(m, q, p->quirks, grad);
+  om_face_flux_ext(m, p, q, grad, F);
+  om_gather(m, F, R);
+}
+
+int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
+                int nsteps, double t_end, double *time, om_norms *last) {
+  const int nC = m->n_cells;
+  double *F = (double *)calloc((size_t)8 * m->n_faces, 8);
+  double *grad = (double *)calloc((size_t)8 * nC, 8);
+  double *R = (double *)calloc((size_t)4 * nC, 8);
+  double *q1 = (double *)calloc((size_t)4 * nC, 8);
+  double *qn = (double *)calloc((size_t)4 * nC, 8);
+  double *dtc = (double *)calloc((size_t)nC, 8);
+  if (!F || !grad || !R || !q1 || !qn || !dtc) {
+    free(F), free(grad), free(R), free(q1), free(qn), free(dtc);
+    return OM_EINVAL;
+  }
+  double t = time ? *time : 0.0;
+  for (int s = 0; s < nsteps; ++s) {
+    if (t_end > 0 && t >= t_end) break; /* further steps would have dt = 0 */
+    double dt = p->dt;
+    if (p->dt_mode != OM_DT_FIXED) dt = om_spectral_dt(m, q, p->cfl, dtc);
+    if (t_end > 0 && t + dt > t_end) dt = t_end - t;
+    if (dt < 0) dt = 0;
+    const int local = (p->dt_mode == OM_DT_CFL_LOCAL);
+    const double *qin = q;
+    double *out = p->rk2 ? q1 : qn;
+    residual_ext(m, p, q, F, grad, R);
+    for (int c = 0; c < nC; ++c) {
+      const double f = (local ? dtc[c] : dt) / m->cell_vol[c];
+      for (int j = 0; j < 4; ++j) out[4 * c + j] = q[4 * c + j] - f * R[4 * c + j];
+    }
+    if (p->rk2) {
+      qin = q1;
+      residual_ext(m, p, q1, F, grad, R);
+      for (int c = 0; c < nC; ++c) {
+        const double f = (local ? dtc[c] : dt) / m->cell_vol[c];
+        for (int j = 0; j < 4; ++j)
+          qn[4 * c + j] = 0.5 * q[4 * c + j] + 0.5 * (q1[4 * c + j] - f * R[4 * c + j]);
+      }
+    }
+    if (last) {
+      memset(last, 0, sizeof *last);
+      for (int c = 0; c < nC; ++c) {
+        const double v = m->cell_vol[c];
+        for (int j = 0; j < 4; ++j) {
+          const double ch = fabs(qn[4 * c + j] - qin[4 * c + j]) / qin[4 * c + j];
+          if (last->linf[j] < ch) last->linf[j] = ch;
+          const double rv = R[4 * c + j] / v;
+          last->l2[j] += rv * rv;
+        }
+        last->mass += v * qn[4 * c];
+      }
+      for (int j = 0; j < 4; ++j) last->l2[j] = sqrt(last->l2[j] / (double)nC);
+      last->dt = dt;
+    }
+    t += dt;
+    memcpy(q, qn, sizeof(double) * 4 * nC);
+  }
+  if (last) last->time = t;
+  if (time) *time = t;
+  free(F), free(grad), free(R), free(q1), free(qn), free(dtc);
+  return OM_OK;
+}

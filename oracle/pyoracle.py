@@ -38,6 +38,18 @@ class _OParams(C.Structure):
                 ("inlet_q", C.c_double * 4)]
 
 
+class _OParamsExt(C.Structure):
+    _fields_ = [("flux", C.c_int), ("order", C.c_int), ("limiter", C.c_int),
+                ("quirks", C.c_int), ("rk2", C.c_int), ("dt_mode", C.c_int),
+                ("dt", C.c_double), ("cfl", C.c_double),
+                ("inlet_q", C.c_double * 4)]
+
+
+class _ONorms(C.Structure):
+    _fields_ = [("linf", C.c_double * 4), ("l2", C.c_double * 4),
+                ("mass", C.c_double), ("dt", C.c_double), ("time", C.c_double)]
+
+
 _lib = None
 
 
@@ -62,6 +74,17 @@ def lib():
         L.om_solve.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParams), _dp,
                                C.c_double, _dp, _dp]
         L.om_linf_change.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.om_mesh_from_arrays_periodic.argtypes = [
+            C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, C.c_int, _ip, _dp,
+            C.POINTER(C.POINTER(_OMesh))]
+        L.om_default_params_ext.argtypes = [C.POINTER(_OParamsExt)]
+        L.om_gradient_ext.argtypes = [C.POINTER(_OMesh), _dp, C.c_int, _dp]
+        L.om_face_flux_ext.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParamsExt),
+                                       _dp, _dp, _dp]
+        L.om_spectral_dt.argtypes = [C.POINTER(_OMesh), _dp, C.c_double, _dp]
+        L.om_spectral_dt.restype = C.c_double
+        L.om_step_ext.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParamsExt), _dp,
+                                  C.c_int, C.c_double, _dp, C.POINTER(_ONorms)]
         _lib = L
     return _lib
 
@@ -130,15 +153,17 @@ def read_msh(path):
     return Mesh(p)
 
 
-def mesh_from_arrays(node_xy, face_nodes, face_cells, zones, n_cells):
+def mesh_from_arrays(node_xy, face_nodes, face_cells, zones, n_cells,
+                     c1_shift=None):
     node_xy = _f64(node_xy)
     fn = np.ascontiguousarray(face_nodes, dtype=np.int32)
     fc = np.ascontiguousarray(face_cells, dtype=np.int32)
     z = np.ascontiguousarray(zones, dtype=np.int32)
+    sh = _f64(c1_shift) if c1_shift is not None else None
     p = C.POINTER(_OMesh)()
-    rc = lib().om_mesh_from_arrays(len(node_xy), _d(node_xy), int(n_cells),
-                                   len(fn), _i(fn), _i(fc), len(z), _i(z),
-                                   C.byref(p))
+    rc = lib().om_mesh_from_arrays_periodic(
+        len(node_xy), _d(node_xy), int(n_cells), len(fn), _i(fn), _i(fc),
+        len(z), _i(z), _d(sh) if sh is not None else _dp(), C.byref(p))
     if rc != 0:
         raise ValueError(f"oracle: bad mesh arrays (status {rc})")
     return Mesh(p)
@@ -205,3 +230,58 @@ def linf_change(qold, qnew):
     r = np.zeros(4)
     lib().om_linf_change(len(qold), _d(qold), _d(qnew), _d(r))
     return r
+
+
+# ---------------------------------------------------------------------------
+# extensions (no reference counterpart): limiters, corrected boundaries,
+# periodic images, CFL steps, two-stage Runge-Kutta
+# ---------------------------------------------------------------------------
+LIM_NONE, LIM_MINMOD, LIM_VANLEER, LIM_VANALBADA = range(4)
+DT_FIXED, DT_CFL_GLOBAL, DT_CFL_LOCAL = range(3)
+
+
+def params_ext(flux=AUSM, order=1, limiter=0, quirks=1, rk2=0, dt_mode=0,
+               dt=1.0 / 4e3, cfl=0.5, inlet_q=None):
+    p = _OParamsExt()
+    lib().om_default_params_ext(C.byref(p))
+    p.flux, p.order, p.limiter, p.quirks, p.rk2 = flux, order, limiter, quirks, rk2
+    p.dt_mode, p.dt, p.cfl = dt_mode, float(dt), float(cfl)
+    if inlet_q is not None:
+        for k in range(4):
+            p.inlet_q[k] = float(inlet_q[k])
+    return p
+
+
+def gradient_ext(mesh, q, quirks):
+    q = _f64(q)
+    g = np.zeros((mesh.n_cells, 2, 4))
+    lib().om_gradient_ext(mesh._p, _d(q), int(quirks), _d(g))
+    return g
+
+
+def face_flux_ext(mesh, prm, q, grad=None):
+    q = _f64(q)
+    F = np.zeros((mesh.n_faces, 2, 4))
+    g = _d(_f64(grad)) if grad is not None else _dp()
+    lib().om_face_flux_ext(mesh._p, C.byref(prm), _d(q), g, _d(F))
+    return F
+
+
+def spectral_dt(mesh, q, cfl):
+    q = _f64(q)
+    d = np.zeros(mesh.n_cells)
+    m = lib().om_spectral_dt(mesh._p, _d(q), float(cfl), _d(d))
+    return m, d
+
+
+def step_ext(mesh, prm, q, nsteps, t_end=0.0, time=0.0):
+    """nsteps steps; returns (q, norms dict of the last step)."""
+    q = _f64(q).copy()
+    t = C.c_double(time)
+    n = _ONorms()
+    rc = lib().om_step_ext(mesh._p, C.byref(prm), _d(q), int(nsteps), float(t_end),
+                           C.byref(t), C.byref(n))
+    if rc != 0:
+        raise RuntimeError("om_step_ext failed")
+    return q, dict(linf_change=np.array(n.linf[:]), l2_resid=np.array(n.l2[:]),
+                   mass=n.mass, dt=n.dt, time=t.value)
