@@ -1,0 +1,340 @@
+"""Benchmark of the density-based residual path on GB300.
+
+Workload (the 2D isentropic-vortex configuration): periodic [0,10]^2,
+jittered Delaunay triangles from an n x n node lattice (n = 1000: 2,000,000
+cells, 3,000,000 faces; node jitter U(-0.25h, 0.25h), seed 20261203),
+vortex of strength 5 convected at Mach 0.5, AUSM+ flux, van Leer limiter,
+two-stage Runge-Kutta at global CFL 0.5.  A step is one RK2 time step
+(two residual evaluations and two state updates of every cell), i.e. two
+cell-updates per cell.  Inputs (state + mesh, ~0.5 GB) exceed the 129 MB L2
+between steps.
+
+Arms:
+  (default)          the CUDA path through the C ABI; value = FP32-flux /
+                     FP64-accumulate Mcell-updates/s with the state resident
+                     in HBM, timed with CUDA events on the context's stream;
+                     "fp64" = the same in FP64; "e2e" = FP32 through the
+                     public API with the state copied host->device and back
+                     every step from page-locked host buffers.
+  --impl reference   the CPU restatement of the same path (the oracle,
+                     OpenMP over all host cores) on the same workload.
+
+One JSON line on rank 0.  Under torchrun each rank runs an independent
+replica on its own GPU (single-mesh runs do not shard: replicas only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mst-cfd_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mcell-updates/s FP32 vs FP64"
+UNIT = "Mcell-updates/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class _Group:
+    """Barrier and max-reduce across ranks (gloo; no data-path collective)."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+class _Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                rows.append((float(f[0]), float(f[1]), f[4:8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r)
+                          if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _workload(n):
+    from mstcfd import meshgen as mg
+    m = mg.periodic_delaunay(n, 10.0, jitter=0.25, seed=20261203)
+    return m
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_traffic(kernel, n_cells):
+    """DRAM bytes per launch of ``kernel`` from the committed ncu summary
+    (per cell, scaled to this mesh), or None."""
+    path = os.path.join(ROOT, "profiles", "flux_update_vortex_ncu.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_cell[" + kernel + "]"):
+            try:
+                return float(line.split("=")[1].split()[0]) * n_cells
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def run_gpu(args, ws, rank, local, grp):
+    from mstcfd import Mesh, PinnedArray, Solver, capi, roofline
+    from mstcfd import meshgen as mg
+    capi.check(capi.load().mst_set_device(local))
+    m = _workload(args.n)
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"], c1_shift=m["c1_shift"])
+    nC = mesh.n_cells
+    q0 = mg.isentropic_vortex(m["cell_centroid"])
+    kw = dict(flux=0, order=2, limiter=2, reference_quirks=0, time_scheme=1,
+              dt_mode=1, cfl=0.5)
+    results = {}
+    prof = {}
+    for prec, label in ((2, "fp32"), (1, "fp64")):
+        steps = args.steps if prec == 2 else max(3, args.steps // 4)
+        s = Solver(mesh, precision=prec, **kw)
+        s.set_state(q0)
+        s.step(args.warmup)
+        clocks = _Clocks(local) if prec == 2 else None
+        grp.barrier()
+        if clocks:
+            clocks.start()
+        s.profile(True)
+        s.step(steps)
+        ms, launches = s.last_timing()
+        s.profile(False)
+        if clocks:
+            results["clocks"] = clocks.stop()
+        grp.barrier()
+        ms_max = grp.max(ms)
+        cells_all = grp.sum(2.0 * nC * steps)
+        results[label] = dict(value=cells_all / (ms_max * 1e-3) / 1e6,
+                              ms_per_step=ms_max / steps, steps=steps,
+                              launches=launches)
+        prof[label] = s.profile_stats()
+        if prec == 2:
+            # end to end through the public API with host buffers
+            hin = PinnedArray((nC, 4))
+            hout = PinnedArray((nC, 4))
+            hin.array[:] = s.state()
+            s.set_state_ptr(hin.ptr)
+            s.step(1)
+            s.get_state_ptr(hout.ptr)
+            grp.barrier()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                s.set_state_ptr(hin.ptr)
+                s.step(1)
+                s.get_state_ptr(hout.ptr)
+            t1 = time.perf_counter()
+            grp.barrier()
+            e2e_s = grp.max(t1 - t0)
+            results["e2e"] = dict(value=cells_all / e2e_s / 1e6, unit=UNIT,
+                                  h2d_bytes_per_step=int(hin.nbytes),
+                                  d2h_bytes_per_step=int(hout.nbytes))
+            if not np.all(np.isfinite(hout.array)):
+                raise RuntimeError("non-finite state after the e2e steps")
+            hin.free()
+            hout.free()
+        s.close()
+    # roofline of the dominant kernel (largest share of the FP32 step)
+    st = prof["fp32"]
+    top = max(st, key=lambda k: st[k][1])
+    n_launch, tot_ms = st[top]
+    avg_ms = tot_ms / n_launch
+    info = mesh.info
+    if top.startswith("k_flux_update"):
+        # launches alternate stage 0 / stage 1
+        b = 0.5 * (roofline.kernel_bytes(info, 2, 2, top, stage=0) +
+                   roofline.kernel_bytes(info, 2, 2, top, stage=1))
+    else:
+        b = roofline.kernel_bytes(info, 2, 2, top)
+    peak, peak_kind = _peaks()
+    achieved = b / (avg_ms * 1e-3) / 1e9
+    traffic = _profile_traffic(top, nC)
+    share = {k: round(v[1] / sum(x[1] for x in st.values()), 4) for k, v in st.items()}
+    return results, dict(bound="hbm", achieved=round(achieved, 1), peak=peak,
+                         unit="GB/s", frac=round(achieved / peak, 4),
+                         traffic=traffic, kernel=top, peak_source=peak_kind,
+                         algorithmic_bytes_per_launch=int(b),
+                         avg_launch_ms=round(avg_ms, 5), kernel_share=share), nC
+
+
+def run_cpu_sample(m, steps, budget_s=30.0):
+    """The oracle port (OpenMP over all host cores) on the workload."""
+    from mstcfd import meshgen as mg
+    from oracle import pyoracle as po
+    om = po.mesh_from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                             m["n_cells"], c1_shift=m["c1_shift"])
+    q = mg.isentropic_vortex(m["cell_centroid"])
+    prm = po.params_ext(0, 2, limiter=2, quirks=0, rk2=1, dt_mode=1, cfl=0.5)
+    q, _ = po.step_ext(om, prm, q, 1)  # warm
+    done, t_total = 0, 0.0
+    while done < steps:
+        t0 = time.perf_counter()
+        q, _ = po.step_ext(om, prm, q, 1)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > budget_s:
+            break
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return 2.0 * m["n_cells"] * done / t_total / 1e6, cores, done, t_total
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mstcfd", choices=["mstcfd", "reference"])
+    ap.add_argument("--n", type=int, default=1000, help="lattice size (n*n*2 cells)")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU-baseline sample (profiler runs)")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    workload = (f"isentropic vortex, periodic jittered Delaunay {args.n}x{args.n} "
+                f"lattice ({2 * args.n * args.n} triangles), AUSM+ + van Leer, "
+                f"RK2, CFL 0.5")
+    config = {"workload": workload, "cells": 2 * args.n * args.n,
+              "faces": 3 * args.n * args.n, "step": "one RK2 time step = 2 cell-updates per cell",
+              "l2": "inputs larger than L2 (state + mesh ~0.5 GB)",
+              "parallelism": f"replicas x{ws}"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import build as ob
+        ob.build_oracle()
+        m = _workload(args.n)
+        from oracle import pyoracle as po  # noqa: F401
+        # warmup steps then timed steps, each one RK2 step of the full mesh,
+        # bounded to a few minutes in total
+        run_cpu_sample(m, max(1, args.warmup), budget_s=20.0)
+        v, cores, done, secs = run_cpu_sample(m, args.steps, budget_s=120.0)
+        line = {"metric": METRIC, "value": round(v, 3), "unit": UNIT, "impl": "reference",
+                "n_gpus": args.gpus, "steps": done, "warmup": args.warmup,
+                "ms_per_step": round(1e3 * secs / done, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores,
+                                 "kind": "port",
+                                 "sample": f"{done} RK2 steps of the full mesh"},
+                "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    grp = _Group(ws)
+    results, roof, nC = run_gpu(args, ws, rank, local, grp)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        m = _workload(args.n)
+        v, cores, done, secs = run_cpu_sample(m, args.cpu_steps, budget_s=25.0)
+        cpu = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{done} RK2 step(s) of the full {m['n_cells']}-cell mesh "
+                         f"({secs:.1f} s, FP64, OpenMP)"}
+    if rank != 0:
+        return
+    fp32, fp64 = results["fp32"], results["fp64"]
+    line = {"metric": METRIC, "value": round(fp32["value"], 2), "unit": UNIT,
+            "n_gpus": ws, "steps": fp32["steps"], "warmup": args.warmup,
+            "ms_per_step": round(fp32["ms_per_step"], 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate",
+            "data": "synthetic", "config": config,
+            "fp64": {"value": round(fp64["value"], 2), "unit": UNIT,
+                     "ms_per_step": round(fp64["ms_per_step"], 5), "dtype": "f64"},
+            "e2e": {k: (round(v, 2) if isinstance(v, float) else v)
+                    for k, v in results["e2e"].items()},
+            "gpu_launches": fp32["launches"],
+            "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks")}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -217,6 +217,8 @@ mst_status mst_host_free(void *p);
 
 /* Number of CUDA devices visible to this process. */
 mst_status mst_device_count(int *n);
+/* Selects the device later contexts of this host thread are created on. */
+mst_status mst_set_device(int device);
 
 /* Text of the last error on this thread (static storage). */
 const char *mst_last_error(void);

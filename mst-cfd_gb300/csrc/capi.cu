@@ -808,6 +808,14 @@ mst_status mst_host_free(void* p) {
   return MST_OK;
 }
 
+mst_status mst_set_device(int device) {
+  int n = 0;
+  CU(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(MST_EINVAL, "no such device");
+  CU(cudaSetDevice(device));
+  return MST_OK;
+}
+
 mst_status mst_device_count(int* n) {
   if (!n) return fail(MST_EINVAL, "NULL argument");
   *n = 0;

@@ -827,6 +827,7 @@ void om_face_flux(const om_mesh *m, const om_params *p, const double *q,
 }
 
 void om_gather(const om_mesh *m, const double *F, double *R) {
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < m->n_cells; ++c) {
     double r[4] = {0, 0, 0, 0};
     for (int k = m->cell_ptr[c]; k < m->cell_ptr[c + 1]; ++k) {

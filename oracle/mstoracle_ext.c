@@ -31,6 +31,7 @@ void om_gradient_ext(const om_mesh *m, const double *q, int quirks,
                      double *grad) {
   const int first = quirks ? (m->n_int_faces > 0 ? m->n_int_faces - 1 : 0)
                            : m->n_int_faces;
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < m->n_cells; ++c) {
     double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = m->cell_ptr[c]; k < m->cell_ptr[c + 1]; ++k) {
@@ -99,6 +100,7 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
   const int limited = second && !p->quirks && p->limiter != OM_LIM_NONE;
   for (int z = 0; z < m->n_zones; ++z) {
     const int type = m->zone[4 * z + 3];
+#pragma omp parallel for schedule(static)
     for (int i = m->zone[4 * z + 1] - 1; i < m->zone[4 * z + 2]; ++i) {
       double *Fi = F + 8 * i;
       const int c0 = m->face_cells[2 * i], c1 = m->face_cells[2 * i + 1];
@@ -172,6 +174,7 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
 double om_spectral_dt(const om_mesh *m, const double *q, double cfl,
                       double *dt_cell) {
   double dmin = 1e300;
+#pragma omp parallel for schedule(static) reduction(min : dmin)
   for (int c = 0; c < m->n_cells; ++c) {
     const double *qs = q + 4 * c;
     const double u = qs[1] / qs[0], v = qs[2] / qs[0];
@@ -223,6 +226,7 @@ int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
     const double *qin = q;
     double *out = p->rk2 ? q1 : qn;
     residual_ext(m, p, q, F, grad, R);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < nC; ++c) {
       const double f = (local ? dtc[c] : dt) / m->cell_vol[c];
       for (int j = 0; j < 4; ++j) out[4 * c + j] = q[4 * c + j] - f * R[4 * c + j];
@@ -230,6 +234,7 @@ int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
     if (p->rk2) {
       qin = q1;
       residual_ext(m, p, q1, F, grad, R);
+#pragma omp parallel for schedule(static)
       for (int c = 0; c < nC; ++c) {
         const double f = (local ? dtc[c] : dt) / m->cell_vol[c];
         for (int j = 0; j < 4; ++j)
