@@ -12,10 +12,10 @@ from .capi import (DT_CFL_GLOBAL, DT_CFL_LOCAL, DT_FIXED, FLUX_AUSM, FLUX_ROE,
                    LIMITER_MINMOD, LIMITER_NONE, LIMITER_VANALBADA,
                    LIMITER_VANLEER, MstError, PREC_FP32, PREC_FP64,
                    PREC_FP64_EXACT, TIME_EULER, TIME_RK2)
-from .solver import Mesh, RhoSolver, Solver
+from .solver import Mesh, PinnedArray, RhoSolver, Solver
 
 __all__ = [
-    "capi", "Mesh", "Solver", "RhoSolver", "MstError",
+    "capi", "Mesh", "Solver", "RhoSolver", "PinnedArray", "MstError",
     "FLUX_AUSM", "FLUX_ROE", "LIMITER_NONE", "LIMITER_MINMOD",
     "LIMITER_VANLEER", "LIMITER_VANALBADA", "PREC_FP64_EXACT", "PREC_FP64",
     "PREC_FP32", "TIME_EULER", "TIME_RK2", "DT_FIXED", "DT_CFL_GLOBAL",
