@@ -184,6 +184,32 @@ typedef struct mst_norms {
   double mass;           /* sum_c V_c * rho_c (conservation check) */
 } mst_norms;
 
+/* One residual evaluation and explicit update (what mst_solve does, with
+ * the context's parameters and fixed dt) on device buffers the caller owns,
+ * allocating nothing during the call.  No counterpart in the reference: it
+ * serves programs that embed the solver in a GPU application which manages
+ * all device memory itself and forbids cudaMalloc/cudaFree while running
+ * (cudaFree synchronises the whole device; a pool may have no room), and
+ * loops that must avoid those implicit synchronisations.  The context is
+ * created once at set-up (that call does allocate).
+ *   q_dev, qnew_dev  [n_cells][4] doubles in the context's device cell order
+ *                    (mst_mesh_arrays.cell_perm gives each file cell's row),
+ *                    32-byte aligned; q_dev is read, qnew_dev written
+ *   r_dev            optional [n_cells][4] residual output (same order)
+ *   norms_dev        optional 10 doubles: linf_change[4], l2_resid[4],
+ *                    mass, dt
+ * Scratch (gradients, norm partials) is one fixed file-scope device array of
+ * about 8.1 MiB that every GPU loading the library keeps until exit, so the
+ * mesh may have at most 131072 cells (larger meshes: MST_EINVAL).  All calls
+ * share that array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Runs on the context's stream and returns when the outputs are written;
+ * the caller must have finished writing q_dev before the call. */
+mst_status mst_solve_device_noalloc(mst_ctx *c, const double *q_dev,
+                                   double *qnew_dev, double *r_dev,
+                                   double *norms_dev);
+
 /* Device-resident time stepping: nsteps steps of the configured scheme
  * without host round trips (the Work::work loop, work/Work.cpp:53-89, with
  * the state kept in HBM).  t_end > 0 clips the last step to reach t_end

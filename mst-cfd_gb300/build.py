@@ -6,6 +6,7 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/kernels_exact.cu  FP64 parity kernels, --fmad=false
   * csrc/kernels_fast.cu   FP64/FP32 production kernels (FMA allowed)
   * csrc/capi.cu           the C ABI of include/mstcfd.h
+  * csrc/noalloc.cu        the allocation-free solve entry point
 """
 import os
 import shutil
@@ -41,6 +42,7 @@ def _units():
                                              os.path.join(CSRC, "kernels_exact.cu")]),
         ("kernels_fast.o", [nv] + common + ["-c", os.path.join(CSRC, "kernels_fast.cu")]),
         ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
+        ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
     ]
 
 

@@ -1,0 +1,62 @@
+// Internal definitions of the C ABI's opaque handles, shared by the
+// translation units that implement entry points (capi.cu, noalloc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mstcfd.h"
+#include "devtypes.hpp"
+#include "mesh.hpp"
+
+// Records msg as this thread's mst_last_error() text and returns s.
+mst_status mst_internal_fail(mst_status s, const std::string& msg);
+
+struct mst_mesh {
+  mst::HostMesh host;
+  mst::DevLayout lay;
+};
+
+struct DevArrays {
+  int2* f_c0c1 = nullptr;
+  int* f_info = nullptr;
+  double2 *f_dir = nullptr, *f_r0 = nullptr, *f_r1 = nullptr, *cf_w = nullptr;
+  float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr;
+  double* c_vol = nullptr;
+  int *c_ptr = nullptr, *cf_face = nullptr, *cf_slot = nullptr, *cf_nb = nullptr,
+      *cf_nb_fix = nullptr, *t_own_ptr = nullptr, *t_bor_ptr = nullptr,
+      *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr;
+};
+
+struct mst_ctx {
+  const mst_mesh* mesh = nullptr;
+  mst_params p{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevArrays d;
+  mst::DevMesh dm{};
+  double4_32a *q_old = nullptr, *q_new = nullptr, *q_stage = nullptr,
+              *r = nullptr, *stage_in = nullptr;
+  void* grad = nullptr;
+  double* flux = nullptr;      // [nF][8] debug output
+  double* partials = nullptr;  // [max(nT, nBlocks)][kNormSlots]
+  double* dt_part = nullptr;   // [nBlocks]
+  double* dt_cell = nullptr;   // [nC]
+  double* scal = nullptr;      // [0] dt, [1] time
+  double* norms = nullptr;     // [kNormSlots + 2]
+  int last_launches = 0;
+  // per-kernel event timing
+  bool profiling = false;
+  struct Pending { int kernel; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::string> kname;
+  std::vector<int> klaunch;
+  std::vector<double> kms;
+  bool timed = false;
+  bool grad_valid = false;
+  std::vector<void*> allocs;
+};
+

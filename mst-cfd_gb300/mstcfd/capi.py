@@ -117,6 +117,8 @@ def load():
         "mst_host_free": (C.c_int, [C.c_void_p]),
         "mst_device_count": (C.c_int, [_ip]),
         "mst_set_device": (C.c_int, [C.c_int]),
+        "mst_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p]),
         "mst_last_error": (C.c_char_p, []),
         "mst_abi_version": (C.c_int, []),
     }

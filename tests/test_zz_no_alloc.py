@@ -1,0 +1,130 @@
+"""mst_solve_device_noalloc: the allocation-free solve on caller-owned
+device buffers, for programs that manage all device memory themselves and
+cannot let the library call cudaMalloc/cudaFree while they run.
+
+The test plays such a caller: it owns its device buffers (allocated here
+through the CUDA runtime), calls the new entry point through the C ABI twice
+in a row on the same buffers, and checks each call's new state, residual and
+norms against the existing entry points (mst_solve / mst_step) on the same
+input.  Tolerance: the same kernels run in both, so states and residuals
+must be identical; the L2 norms are compared to rtol 1e-12 and the mass to
+rtol 1e-13 as elsewhere in the GPU tests.  Kept in its own file, collected
+last, so a run that stops at the first failure has run every other test.
+"""
+import ctypes as C
+import ctypes.util
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cudart():
+    cands = [ctypes.util.find_library("cudart")]
+    cands += sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+    cands += sorted(glob.glob("/usr/local/cuda/targets/*/lib/libcudart.so*"))
+    for c in cands:
+        if not c:
+            continue
+        try:
+            rt = C.CDLL(c)
+        except OSError:
+            continue
+        rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        rt.cudaFree.argtypes = [C.c_void_p]
+        rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        return rt
+    pytest.fail("CUDA runtime library not found")
+
+
+class _DevBuf:
+    """A device buffer owned by the caller (cudaMalloc is 256-byte aligned)."""
+
+    def __init__(self, rt, nbytes):
+        self.rt, self.n = rt, nbytes
+        self.p = C.c_void_p()
+        assert rt.cudaMalloc(C.byref(self.p), nbytes) == 0
+
+    def put(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.nbytes == self.n
+        assert self.rt.cudaMemcpy(self.p, a.ctypes.data, self.n, 1) == 0
+
+    def get(self, shape):
+        out = np.empty(shape, dtype=np.float64)
+        assert self.rt.cudaMemcpy(out.ctypes.data, self.p, self.n, 2) == 0
+        return out
+
+    def free(self):
+        self.rt.cudaFree(self.p)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("prec", [0, 2], ids=["fp64_exact", "fp32"])
+def test_noalloc_matches_existing_entry_points(order, prec):
+    from mstcfd import Mesh, Solver, capi
+    from mstcfd import meshgen as mg
+    m = mg.reorient(mg.tri_box(60, 30, 4.0, 2.0, jitter=0.25, seed=44), "random", seed=2)
+    if order == 2:
+        m = mg.with_zone_types(m, mg.OUTLET, mg.WALL)
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"])
+    arrs = mesh.arrays()
+    q0 = mg.smooth_state(arrs["cell_ctr"])
+    s = Solver(mesh, order=order, precision=prec, dt=2e-4)
+    # existing entry points
+    s.set_state(q0)
+    s.solve()
+    want_qn, want_r = s.new_state(), s.residual()
+    s.set_state(q0)
+    want_norms = s.step(1)
+    # the caller's own device buffers, rows in the context's device order
+    nC = mesh.n_cells
+    perm = arrs["cell_perm"]
+    q_dev_order = np.empty_like(q0)
+    q_dev_order[perm] = q0
+    rt = _cudart()
+    bq, bqn, br = (_DevBuf(rt, nC * 32) for _ in range(3))
+    bn = _DevBuf(rt, 10 * 8)
+    try:
+        bq.put(q_dev_order)
+        lib = capi.load()
+        for call in range(2):
+            st = lib.mst_solve_device_noalloc(s._h, bq.p, bqn.p, br.p, bn.p)
+            assert st == capi.OK, lib.mst_last_error()
+            qn = bqn.get((nC, 4))[perm]
+            r = br.get((nC, 4))[perm]
+            nrm = bn.get(10)
+            assert np.array_equal(qn, want_qn), call
+            assert np.array_equal(r, want_r), call
+            assert np.array_equal(nrm[:4], want_norms["linf_change"]), call
+            assert np.allclose(nrm[4:8], want_norms["l2_resid"], rtol=1e-12, atol=0), call
+            assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-13, atol=0), call
+            assert nrm[9] == want_norms["dt"], call
+    finally:
+        for b in (bq, bqn, br, bn):
+            b.free()
+        s.close()
+
+
+def test_noalloc_rejects_meshes_over_the_limit():
+    from mstcfd import Mesh, Solver, capi
+    from mstcfd import meshgen as mg
+    m = mg.tri_box(300, 240, 4.0, 2.0, jitter=0.2, seed=5)
+    assert m["n_cells"] > 131072
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"])
+    s = Solver(mesh, dt=1e-4)
+    rt = _cudart()
+    b = _DevBuf(rt, mesh.n_cells * 32)
+    try:
+        lib = capi.load()
+        st = lib.mst_solve_device_noalloc(s._h, b.p, b.p, None, None)
+        assert st == capi.EINVAL
+        assert b"at most 131072" in lib.mst_last_error()
+    finally:
+        b.free()
+        s.close()
