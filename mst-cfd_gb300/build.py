@@ -40,7 +40,11 @@ def _units():
                     "-Wall", "-c", os.path.join(CSRC, "mesh.cpp")]),
         ("kernels_exact.o", [nv] + common + ["--fmad=false", "-c",
                                              os.path.join(CSRC, "kernels_exact.cu")]),
-        ("kernels_fast.o", [nv] + common + ["-c", os.path.join(CSRC, "kernels_fast.cu")]),
+        # single-precision division / square root to within 2 ulp and flush of
+        # denormals on the production kernels (no effect on FP64 arithmetic)
+        ("kernels_fast.o", [nv] + common + ["-prec-div=false", "-prec-sqrt=false",
+                                            "-ftz=true", "-c",
+                                            os.path.join(CSRC, "kernels_fast.cu")]),
         ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
         ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
     ]

@@ -80,11 +80,11 @@ __global__ void k_finalize_dt(const double* __restrict__ part, int n,
     if (t_end > 0 && t + x > t_end) x = t_end - t;
     if (x < 0) x = 0;
     scal[0] = x;
+    scal[1] = t + x;  // the step is always taken with this length
   }
 }
 
-// norms of a step from per-tile partials (fixed order: deterministic);
-// advances the simulated time by scal[0] when advance != 0.
+// norms of a step from per-tile partials (fixed order: deterministic).
 // out: linf[4], l2[4] (sqrt(mean)), mass, dt, time
 __global__ void k_finalize_norms(const double* __restrict__ part, int n_tiles,
                                  int n_cells, int advance,
@@ -112,7 +112,7 @@ __global__ void k_finalize_norms(const double* __restrict__ part, int n_tiles,
   }
   __syncthreads();
   if (threadIdx.x == 0 && j == 0) {
-    if (advance) scal[1] += scal[0];
+    (void)advance;
     out[kNormSlots] = scal[0];
     out[kNormSlots + 1] = scal[1];
   }
@@ -199,13 +199,19 @@ void drain_profile(mst_ctx* c) {
   c->pending.clear();
 }
 
-mst_status launch_grad(mst_ctx* c, const double4_32a* q) {
+// gradient of q (qf: its FP32 copy on the FP32 path); with dt_part it also
+// writes the CFL step partials (and dt_cell)
+mst_status launch_grad(mst_ctx* c, const double4_32a* q, const float4* qf = nullptr,
+                       double* dt_part = nullptr, double* dt_cell = nullptr) {
   ProfScope ps(c, c->p.precision == MST_PREC_FP32 ? "k_gradient<f32>" : "k_gradient<f64>");
+  if (c->p.precision != MST_PREC_FP32) qf = nullptr;
   cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
-                      ? mst::exact::launch_gradient(prec_of(c->p), c->dm, q, c->grad,
-                                                    c->p.reference_quirks, c->stream)
-                      : mst::fast::launch_gradient(prec_of(c->p), c->dm, q, c->grad,
-                                                   c->p.reference_quirks, c->stream);
+                      ? mst::exact::launch_gradient_dt(prec_of(c->p), c->dm, q, qf, c->grad,
+                                                       c->p.reference_quirks, c->p.cfl,
+                                                       dt_cell, dt_part, c->stream)
+                      : mst::fast::launch_gradient_dt(prec_of(c->p), c->dm, q, qf, c->grad,
+                                                      c->p.reference_quirks, c->p.cfl,
+                                                      dt_cell, dt_part, c->stream);
   c->last_launches++;
   if (e != cudaSuccess) return fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
   c->grad_valid = true;
@@ -237,13 +243,17 @@ mst::StepArgs base_args(mst_ctx* c) {
 // one residual evaluation + update of stage 'stage' from q into qn
 mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
                      double4_32a* qn, int stage, bool fixed_dt, bool norms,
-                     bool keep_residual) {
-  if (c->p.order == 2) {
-    mst_status s = launch_grad(c, q);
+                     bool keep_residual, const float4* qf = nullptr,
+                     float4* qfn = nullptr, bool grad_ready = false) {
+  if (c->p.precision != MST_PREC_FP32) qf = nullptr, qfn = nullptr;
+  if (c->p.order == 2 && !grad_ready) {
+    mst_status s = launch_grad(c, q, qf);
     if (s) return s;
   }
   mst::StepArgs a = base_args(c);
   a.q = q;
+  a.qf = qf;
+  a.qfn = qfn;
   a.q0 = q0;
   a.qn = qn;
   a.r_out = keep_residual ? c->r : nullptr;
@@ -256,10 +266,20 @@ mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
   return launch_flux(c, a);
 }
 
-mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end) {
+// step length of the next step into scal[0] (and advances the time); on
+// 2nd order the CFL step comes from the stage-0 gradient launch, which is
+// then marked ready (*grad_ready)
+mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end,
+                      const float4* qf = nullptr, bool* grad_ready = nullptr) {
   const int nC = c->dm.n_cells;
   int mode = 0;
-  if (c->p.dt_mode != MST_DT_FIXED) {
+  if (c->p.dt_mode != MST_DT_FIXED && c->p.order == 2 && grad_ready) {
+    mst_status st = launch_grad(c, q, qf, c->dt_part,
+                                c->p.dt_mode == MST_DT_CFL_LOCAL ? c->dt_cell : nullptr);
+    if (st) return st;
+    *grad_ready = true;
+    mode = 1;
+  } else if (c->p.dt_mode != MST_DT_FIXED) {
     ProfScope ps(c, "k_spectral_dt");
     cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                         ? mst::exact::launch_spectral_dt(prec_of(c->p), c->dm, q, c->p.cfl,
@@ -485,6 +505,9 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
     CU(up(&d.f_r1_32, as_f2(L.f_r1)));
     CU(up(&d.cf_w32, as_f2(L.cf_w)));
     CU(up(&d.c_vol, L.c_vol));
+    std::vector<double> ivol(L.c_vol.size());
+    for (size_t i = 0; i < ivol.size(); ++i) ivol[i] = 1.0 / L.c_vol[i];
+    CU(up(&d.c_ivol, ivol));
     CU(up(&d.c_ptr, L.c_ptr));
     CU(up(&d.cf_face, L.cf_face));
     CU(up(&d.cf_slot, L.cf_slot));
@@ -510,6 +533,7 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.f_r0_32 = d.f_r0_32;
   dm.f_r1_32 = d.f_r1_32;
   dm.c_vol = d.c_vol;
+  dm.c_ivol = d.c_ivol;
   dm.c_ptr = d.c_ptr;
   dm.cf_face = d.cf_face;
   dm.cf_slot = d.cf_slot;
@@ -525,6 +549,9 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   if ((st = dalloc(c.get(), &c->q_old, qbytes)) || (st = dalloc(c.get(), &c->q_new, qbytes)) ||
       (st = dalloc(c.get(), &c->q_stage, qbytes)) || (st = dalloc(c.get(), &c->r, qbytes)) ||
       (st = dalloc(c.get(), &c->stage_in, qbytes)) ||
+      (st = dalloc(c.get(), &c->qf_old, nC * sizeof(float4))) ||
+      (st = dalloc(c.get(), &c->qf_new, nC * sizeof(float4))) ||
+      (st = dalloc(c.get(), &c->qf_stage, nC * sizeof(float4))) ||
       (st = dalloc(c.get(), (char**)&c->grad, nC * 8 * sizeof(double))) ||
       (st = dalloc(c.get(), &c->partials,
                    std::max<size_t>(L.n_tiles, nB) * kNormSlots * sizeof(double))) ||
@@ -563,8 +590,14 @@ mst_status mst_ctx_set_params(mst_ctx* c, const mst_params* p) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   mst_status st = check_params(p);
   if (st) return st;
+  const bool to_f32 = p->precision == MST_PREC_FP32 && c->p.precision != MST_PREC_FP32;
   c->p = *p;
   c->grad_valid = false;
+  if (to_f32) {  // the FP32 copies of the state were not maintained so far
+    CU(mst::fast::launch_to_f32(c->q_old, c->qf_old, c->dm.n_cells, c->stream));
+    CU(mst::fast::launch_to_f32(c->q_new, c->qf_new, c->dm.n_cells, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  }
   return MST_OK;
 }
 
@@ -586,6 +619,11 @@ mst_status mst_set_state(mst_ctx* c, const double* q, size_t stride) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(c->q_new, c->q_old, (size_t)nC * sizeof(double4_32a),
                      cudaMemcpyDeviceToDevice, c->stream));
+  if (c->p.precision == MST_PREC_FP32) {
+    CU(mst::fast::launch_to_f32(c->q_old, c->qf_old, nC, c->stream));
+    CU(cudaMemcpyAsync(c->qf_new, c->qf_old, (size_t)nC * sizeof(float4),
+                       cudaMemcpyDeviceToDevice, c->stream));
+  }
   CU(cudaStreamSynchronize(c->stream));
   c->grad_valid = false;
   return MST_OK;
@@ -613,7 +651,8 @@ mst_status mst_solve(mst_ctx* c) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   c->last_launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
-  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true, true);
+  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true, true, c->qf_old,
+                           c->qf_new);
   if (s) return s;
   if ((s = finalize_norms(c, false))) return s;
   CU(cudaEventRecord(c->ev1, c->stream));
@@ -627,6 +666,9 @@ mst_status mst_update_new_to_old(mst_ctx* c) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   CU(cudaMemcpyAsync(c->q_old, c->q_new, (size_t)c->dm.n_cells * sizeof(double4_32a),
                      cudaMemcpyDeviceToDevice, c->stream));
+  if (c->p.precision == MST_PREC_FP32)
+    CU(cudaMemcpyAsync(c->qf_old, c->qf_new, (size_t)c->dm.n_cells * sizeof(float4),
+                       cudaMemcpyDeviceToDevice, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   c->grad_valid = false;
   return MST_OK;
@@ -694,17 +736,25 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
   c->last_launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
   for (int s = 0; s < nsteps; ++s) {
-    mst_status st = compute_dt(c, c->q_old, t_end);
+    // norms (per-tile partials + one reduction) on the last step only
+    const bool norms = (s == nsteps - 1);
+    bool grad_ready = false;
+    mst_status st = compute_dt(c, c->q_old, t_end, c->qf_old, &grad_ready);
     if (st) return st;
     if (c->p.time_scheme == MST_TIME_EULER) {
-      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, true, false);
+      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, norms, false, c->qf_old,
+                     c->qf_new, grad_ready);
     } else {
-      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false, false);
-      if (!st) st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, true, false);
+      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false, false, c->qf_old,
+                     c->qf_stage, grad_ready);
+      if (!st)
+        st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, norms, false,
+                       c->qf_stage, c->qf_new);
     }
     if (st) return st;
-    if ((st = finalize_norms(c, true))) return st;
+    if (norms && (st = finalize_norms(c, true))) return st;
     std::swap(c->q_old, c->q_new);
+    std::swap(c->qf_old, c->qf_new);
   }
   CU(cudaEventRecord(c->ev1, c->stream));
   c->timed = true;

@@ -20,6 +20,7 @@ struct DevMesh {
   const float2* f_r0_32;
   const float2* f_r1_32;
   const double* c_vol;
+  const double* c_ivol;  // 1/V (production paths; the exact path divides)
   const int* c_ptr;
   const int* cf_face;
   const int* cf_slot;
@@ -37,6 +38,8 @@ constexpr int kNormSlots = 9;
 
 struct StepArgs {
   const double4_32a* q;   // state the residual is evaluated on
+  const float4* qf;       // its FP32 copy (FP32 path; nullptr: convert q)
+  float4* qfn;            // FP32 copy of the updated state (or nullptr)
   const double4_32a* q0;  // Q^n for the second RK stage (else nullptr)
   double4_32a* qn;        // updated state
   const void* grad;       // [n_cells][2][4] in the path's precision
@@ -61,6 +64,13 @@ enum { kFluxAusm = 0, kFluxRoe = 1 };
   cudaError_t launch_gradient(int prec, const DevMesh& m,                     \
                               const double4_32a* q, void* grad, int quirks,   \
                               cudaStream_t s);                                \
+  cudaError_t launch_gradient_dt(int prec, const DevMesh& m,                  \
+                                 const double4_32a* q, const float4* qf,      \
+                                 void* grad, int quirks, double cfl,          \
+                                 double* dt_cell, double* dt_part,            \
+                                 cudaStream_t s);                             \
+  cudaError_t launch_to_f32(const double4_32a* q, float4* qf, int n,         \
+                            cudaStream_t s);                                  \
   cudaError_t launch_flux_update(int prec, int flux, int order,              \
                                  const DevMesh& m, const StepArgs& a,         \
                                  int threads, cudaStream_t s);                \

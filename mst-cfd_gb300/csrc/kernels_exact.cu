@@ -6,11 +6,21 @@
 
 namespace mst {
 namespace exact {
+constexpr bool kExactArith = true;
 #include "kernels.inc"
 
 cudaError_t launch_gradient(int, const DevMesh& m, const double4_32a* q,
                             void* grad, int quirks, cudaStream_t s) {
-  return gradient_t<double>(m, q, grad, quirks, s);
+  return gradient_t<double>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, s);
+}
+cudaError_t launch_gradient_dt(int, const DevMesh& m, const double4_32a* q,
+                               const float4*, void* grad, int quirks, double cfl,
+                               double* dt_cell, double* dt_part, cudaStream_t s) {
+  return gradient_t<double>(m, q, nullptr, grad, quirks, cfl, dt_cell, dt_part, s);
+}
+cudaError_t launch_to_f32(const double4_32a* q, float4* qf, int n, cudaStream_t s) {
+  k_to_f32<<<(n + 255) / 256, 256, 0, s>>>(q, qf, n);
+  return cudaGetLastError();
 }
 cudaError_t launch_flux_update(int, int flux, int order, const DevMesh& m,
                                const StepArgs& a, int, cudaStream_t s) {

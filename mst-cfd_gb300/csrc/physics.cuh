@@ -32,26 +32,44 @@ __host__ __device__ __forceinline__ T th_ht(const T q[4]) {
   return (q[3] + p) / q[0];
 }
 
-// AUSM+ flux of the split-axis scheme along axis d (0 = x, 1 = y).
+// Per-state quantities of the AUSM+ flux that do not depend on the axis
+// (SolverAusm.cpp:6-25 set(), :107-113): pressure, total enthalpy, the
+// critical-speed interface estimate a*^2/max(a*,|U|), the true sound speed,
+// and the convected vector (rho, rho u, rho v, rho H).  Computing them once
+// per face state and reusing them for both axes gives the same values as
+// the reference's per-axis recomputation.
 template <class T>
-__host__ __device__ __forceinline__ void ausm_flux(const T ql[4], const T qr[4],
-                                                   int d, T f[4]) {
+struct AusmSide {
+  T p, a_face, a_true, fc[4];
+};
+
+template <class T>
+__host__ __device__ __forceinline__ AusmSide<T> ausm_side(const T q[4]) {
   const T g = Gas<T>::gamma(), gm1 = Gas<T>::gm1(), gp1 = Gas<T>::gp1();
-  const T pL = th_p(ql), pR = th_p(qr);
-  const T hL = (ql[3] + pL) / ql[0], hR = (qr[3] + pR) / qr[0];
-  // interface speed from the critical speeds a* (SolverAusm.cpp:6-22)
-  T aLs = sqrt(T(2) * hL * gm1 / gp1);
-  T aRs = sqrt(T(2) * hR * gm1 / gp1);
-  T UL = sqrt((ql[1] * ql[1] + ql[2] * ql[2]) / ql[0] / ql[0]);
-  T UR = sqrt((qr[1] * qr[1] + qr[2] * qr[2]) / qr[0] / qr[0]);
-  T aL = aLs * aLs / (aLs < UL ? UL : aLs);
-  T aR = aRs * aRs / (aRs < UR ? UR : aRs);
-  T aF = (aR < aL) ? aR : aL;
+  AusmSide<T> s;
+  s.p = th_p(q);
+  const T h = (q[3] + s.p) / q[0];
+  const T as = sqrt(T(2) * h * gm1 / gp1);
+  const T U = sqrt((q[1] * q[1] + q[2] * q[2]) / q[0] / q[0]);
+  s.a_face = as * as / (as < U ? U : as);
+  s.a_true = sqrt(g * s.p / q[0]);
+  s.fc[0] = q[0];
+  s.fc[1] = q[1];
+  s.fc[2] = q[2];
+  s.fc[3] = q[3] + s.p;
+  return s;
+}
+
+// AUSM+ flux along axis d (0 = x, 1 = y) from the two sides' quantities;
+// ql, qr are the states themselves (for the Mach numbers).
+template <class T>
+__host__ __device__ __forceinline__ void ausm_axis(const T ql[4], const AusmSide<T>& L,
+                                                   const T qr[4], const AusmSide<T>& R,
+                                                   int d, T f[4]) {
+  const T aF = (R.a_face < L.a_face) ? R.a_face : L.a_face;
   const T mL = ql[d + 1] / ql[0] / aF;
   const T mR = qr[d + 1] / qr[0] / aF;
-  // flux weights from the true sound speeds (SolverAusm.cpp:112-113)
-  aL = sqrt(g * pL / ql[0]);
-  aR = sqrt(g * pR / qr[0]);
+  const T pL = L.p, pR = R.p, aL = L.a_true, aR = R.a_true;
   T mp, mm, pp, pm;
   // the reference's abs(mach <= 1) is the plain test mach <= 1
   if (mL <= T(1)) {
@@ -75,15 +93,21 @@ __host__ __device__ __forceinline__ void ausm_flux(const T ql[4], const T qr[4],
   const T mF = mm + mp;
   const T pF = pm + pp;
   const T amF = fabs(mF);
-  const T fL[4] = {ql[0], ql[1], ql[2], ql[3] + pL};
-  const T fR[4] = {qr[0], qr[1], qr[2], qr[3] + pR};
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    T a = mF * (aL * fL[k] + aR * fR[k]);
-    T b = amF * (aR * fR[k] - aL * fL[k]);
+    T a = mF * (aL * L.fc[k] + aR * R.fc[k]);
+    T b = amF * (aR * R.fc[k] - aL * L.fc[k]);
     f[k] = T(0.5) * (a - b);
   }
   f[d + 1] += pF;
+}
+
+// AUSM+ flux of the split-axis scheme along axis d (0 = x, 1 = y).
+template <class T>
+__host__ __device__ __forceinline__ void ausm_flux(const T ql[4], const T qr[4],
+                                                   int d, T f[4]) {
+  const AusmSide<T> L = ausm_side(ql), R = ausm_side(qr);
+  ausm_axis(ql, L, qr, R, d, f);
 }
 
 template <class T>
