@@ -53,6 +53,29 @@ __global__ void k_gather_rows(const double4_32a* __restrict__ src,
   if (i < n) dst[i] = src[idx[i]];
 }
 
+// double state <-> float pairs (hi = (float)q, lo = (float)(q - hi)); both
+// in device order
+__global__ void k_to_pairs(const double4_32a* __restrict__ q, float4* __restrict__ hi,
+                           float4* __restrict__ lo, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a v = q[i];
+  const float4 h = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+  hi[i] = h;
+  lo[i] = make_float4((float)(v.x - (double)h.x), (float)(v.y - (double)h.y),
+                      (float)(v.z - (double)h.z), (float)(v.w - (double)h.w));
+}
+// pairs -> double, gathered through idx (idx = nullptr: same order)
+__global__ void k_from_pairs(const float4* __restrict__ hi, const float4* __restrict__ lo,
+                             const int* __restrict__ idx, double4_32a* __restrict__ q, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = idx ? idx[i] : i;
+  const float4 h = hi[s], l = lo[s];
+  q[i] = make_double4_32a((double)h.x + (double)l.x, (double)h.y + (double)l.y,
+                          (double)h.z + (double)l.z, (double)h.w + (double)l.w);
+}
+
 // step length: fixed (mode 0) or min over block partials (mode 1), clipped
 // so that the time reaches t_end; writes scal[0] = dt
 __global__ void k_finalize_dt(const double* __restrict__ part, int n,
@@ -81,6 +104,10 @@ __global__ void k_finalize_dt(const double* __restrict__ part, int n,
     if (x < 0) x = 0;
     scal[0] = x;
     scal[1] = t + x;  // the step is always taken with this length
+    // the same step as a float pair for the FP32 path (scal[2] as 2 floats)
+    float* ff = reinterpret_cast<float*>(scal + 2);
+    ff[0] = (float)x;
+    ff[1] = (float)(x - (double)ff[0]);
   }
 }
 
@@ -230,6 +257,27 @@ mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
   return MST_OK;
 }
 
+bool pairs(const mst_ctx* c) { return c->p.precision == MST_PREC_FP32; }
+
+// double copies of the float-pair states (device order) for the entry
+// points that read the FP64 buffers
+mst_status sync_double_from_pairs(mst_ctx* c) {
+  if (!pairs(c)) return MST_OK;
+  const int n = c->dm.n_cells, nb = (n + 255) / 256;
+  k_from_pairs<<<nb, 256, 0, c->stream>>>(c->qf_old, c->ql_old, nullptr, c->q_old, n);
+  k_from_pairs<<<nb, 256, 0, c->stream>>>(c->qf_new, c->ql_new, nullptr, c->q_new, n);
+  CU(cudaGetLastError());
+  return MST_OK;
+}
+
+mst_status sync_pairs_from_double(mst_ctx* c) {
+  const int n = c->dm.n_cells, nb = (n + 255) / 256;
+  k_to_pairs<<<nb, 256, 0, c->stream>>>(c->q_old, c->qf_old, c->ql_old, n);
+  k_to_pairs<<<nb, 256, 0, c->stream>>>(c->q_new, c->qf_new, c->ql_new, n);
+  CU(cudaGetLastError());
+  return MST_OK;
+}
+
 mst::StepArgs base_args(mst_ctx* c) {
   mst::StepArgs a{};
   a.grad = c->grad;
@@ -241,11 +289,22 @@ mst::StepArgs base_args(mst_ctx* c) {
 }
 
 // one residual evaluation + update of stage 'stage' from q into qn
-mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
-                     double4_32a* qn, int stage, bool fixed_dt, bool norms,
-                     bool keep_residual, const float4* qf = nullptr,
-                     float4* qfn = nullptr, bool grad_ready = false) {
-  if (c->p.precision != MST_PREC_FP32) qf = nullptr, qfn = nullptr;
+// Buffers of one stage: FP64 state q -> qn (q0 = Q^n for stage 1); on the
+// FP32 path the float-pair state (qf, ql) -> (qfn, qln) with (q0f, q0l).
+struct StageBufs {
+  const double4_32a *q = nullptr, *q0 = nullptr;
+  double4_32a* qn = nullptr;
+  const float4 *qf = nullptr, *ql = nullptr, *q0f = nullptr, *q0l = nullptr;
+  float4 *qfn = nullptr, *qln = nullptr;
+};
+
+mst_status run_stage(mst_ctx* c, const StageBufs& b, int stage, bool fixed_dt, bool norms,
+                     bool keep_residual, bool grad_ready = false) {
+  const double4_32a* q = b.q;
+  const double4_32a* q0 = b.q0;
+  double4_32a* qn = b.qn;
+  const float4* qf = pairs(c) ? b.qf : nullptr;
+  float4* qfn = pairs(c) ? b.qfn : nullptr;
   if (c->p.order == 2 && !grad_ready) {
     mst_status s = launch_grad(c, q, qf);
     if (s) return s;
@@ -254,6 +313,15 @@ mst_status run_stage(mst_ctx* c, const double4_32a* q, const double4_32a* q0,
   a.q = q;
   a.qf = qf;
   a.qfn = qfn;
+  if (pairs(c)) {
+    a.qlo = b.ql;
+    a.qlon = b.qln;
+    a.q0f = b.q0f;
+    a.q0lo = b.q0l;
+    a.dt_ff[0] = (float)c->p.dt;
+    a.dt_ff[1] = (float)(c->p.dt - (double)a.dt_ff[0]);
+    if (!fixed_dt) a.dt_ff_dev = reinterpret_cast<const float*>(c->scal + 2);
+  }
   a.q0 = q0;
   a.qn = qn;
   a.r_out = keep_residual ? c->r : nullptr;
@@ -331,10 +399,14 @@ mst_status dalloc(mst_ctx* c, T** p, size_t bytes) {
 }
 
 mst_status download_rows(mst_ctx* c, const double4_32a* dev, double* host,
-                         size_t stride) {
+                         size_t stride, const float4* hi = nullptr,
+                         const float4* lo = nullptr) {
   const int nC = c->dm.n_cells;
   // device order -> file order with a gather by cell_perm, then one copy
-  k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(dev, c->d.cell_perm, c->stage_in, nC);
+  if (hi)
+    k_from_pairs<<<(nC + 255) / 256, 256, 0, c->stream>>>(hi, lo, c->d.cell_perm, c->stage_in, nC);
+  else
+    k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(dev, c->d.cell_perm, c->stage_in, nC);
   CU(cudaGetLastError());
   CU(cudaMemcpy2DAsync(host, stride * sizeof(double), c->stage_in, 4 * sizeof(double),
                        4 * sizeof(double), nC, cudaMemcpyDeviceToHost, c->stream));
@@ -508,6 +580,12 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
     std::vector<double> ivol(L.c_vol.size());
     for (size_t i = 0; i < ivol.size(); ++i) ivol[i] = 1.0 / L.c_vol[i];
     CU(up(&d.c_ivol, ivol));
+    std::vector<float2> ivff(ivol.size());
+    for (size_t i = 0; i < ivol.size(); ++i) {
+      const float h = (float)ivol[i];
+      ivff[i] = make_float2(h, (float)(ivol[i] - (double)h));
+    }
+    CU(up(&d.c_ivol_ff, ivff));
     CU(up(&d.c_ptr, L.c_ptr));
     CU(up(&d.cf_face, L.cf_face));
     CU(up(&d.cf_slot, L.cf_slot));
@@ -534,6 +612,7 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.f_r1_32 = d.f_r1_32;
   dm.c_vol = d.c_vol;
   dm.c_ivol = d.c_ivol;
+  dm.c_ivol_ff = d.c_ivol_ff;
   dm.c_ptr = d.c_ptr;
   dm.cf_face = d.cf_face;
   dm.cf_slot = d.cf_slot;
@@ -552,6 +631,9 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
       (st = dalloc(c.get(), &c->qf_old, nC * sizeof(float4))) ||
       (st = dalloc(c.get(), &c->qf_new, nC * sizeof(float4))) ||
       (st = dalloc(c.get(), &c->qf_stage, nC * sizeof(float4))) ||
+      (st = dalloc(c.get(), &c->ql_old, nC * sizeof(float4))) ||
+      (st = dalloc(c.get(), &c->ql_new, nC * sizeof(float4))) ||
+      (st = dalloc(c.get(), &c->ql_stage, nC * sizeof(float4))) ||
       (st = dalloc(c.get(), (char**)&c->grad, nC * 8 * sizeof(double))) ||
       (st = dalloc(c.get(), &c->partials,
                    std::max<size_t>(L.n_tiles, nB) * kNormSlots * sizeof(double))) ||
@@ -590,14 +672,19 @@ mst_status mst_ctx_set_params(mst_ctx* c, const mst_params* p) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   mst_status st = check_params(p);
   if (st) return st;
-  const bool to_f32 = p->precision == MST_PREC_FP32 && c->p.precision != MST_PREC_FP32;
+  const bool was = pairs(c);
+  const bool to_pairs = p->precision == MST_PREC_FP32 && !was;
+  if (was && p->precision != MST_PREC_FP32) {  // the FP64 buffers were not kept
+    mst_status s = sync_double_from_pairs(c);
+    if (s) return s;
+  }
   c->p = *p;
   c->grad_valid = false;
-  if (to_f32) {  // the FP32 copies of the state were not maintained so far
-    CU(mst::fast::launch_to_f32(c->q_old, c->qf_old, c->dm.n_cells, c->stream));
-    CU(mst::fast::launch_to_f32(c->q_new, c->qf_new, c->dm.n_cells, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
+  if (to_pairs) {
+    mst_status s = sync_pairs_from_double(c);
+    if (s) return s;
   }
+  CU(cudaStreamSynchronize(c->stream));
   return MST_OK;
 }
 
@@ -619,10 +706,9 @@ mst_status mst_set_state(mst_ctx* c, const double* q, size_t stride) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(c->q_new, c->q_old, (size_t)nC * sizeof(double4_32a),
                      cudaMemcpyDeviceToDevice, c->stream));
-  if (c->p.precision == MST_PREC_FP32) {
-    CU(mst::fast::launch_to_f32(c->q_old, c->qf_old, nC, c->stream));
-    CU(cudaMemcpyAsync(c->qf_new, c->qf_old, (size_t)nC * sizeof(float4),
-                       cudaMemcpyDeviceToDevice, c->stream));
+  if (pairs(c)) {
+    mst_status s = sync_pairs_from_double(c);
+    if (s) return s;
   }
   CU(cudaStreamSynchronize(c->stream));
   c->grad_valid = false;
@@ -632,12 +718,14 @@ mst_status mst_set_state(mst_ctx* c, const double* q, size_t stride) {
 mst_status mst_get_state(mst_ctx* c, double* q, size_t stride) {
   if (!c || !q) return fail(MST_EINVAL, "NULL argument");
   if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  if (pairs(c)) return download_rows(c, nullptr, q, stride, c->qf_old, c->ql_old);
   return download_rows(c, c->q_old, q, stride);
 }
 
 mst_status mst_get_new_state(mst_ctx* c, double* q, size_t stride) {
   if (!c || !q) return fail(MST_EINVAL, "NULL argument");
   if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
+  if (pairs(c)) return download_rows(c, nullptr, q, stride, c->qf_new, c->ql_new);
   return download_rows(c, c->q_new, q, stride);
 }
 
@@ -651,8 +739,14 @@ mst_status mst_solve(mst_ctx* c) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   c->last_launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
-  mst_status s = run_stage(c, c->q_old, nullptr, c->q_new, 0, true, true, true, c->qf_old,
-                           c->qf_new);
+  StageBufs b;
+  b.q = c->q_old;
+  b.qn = c->q_new;
+  b.qf = c->qf_old;
+  b.ql = c->ql_old;
+  b.qfn = c->qf_new;
+  b.qln = c->ql_new;
+  mst_status s = run_stage(c, b, 0, true, true, true);
   if (s) return s;
   if ((s = finalize_norms(c, false))) return s;
   CU(cudaEventRecord(c->ev1, c->stream));
@@ -666,9 +760,12 @@ mst_status mst_update_new_to_old(mst_ctx* c) {
   if (!c) return fail(MST_EINVAL, "NULL context");
   CU(cudaMemcpyAsync(c->q_old, c->q_new, (size_t)c->dm.n_cells * sizeof(double4_32a),
                      cudaMemcpyDeviceToDevice, c->stream));
-  if (c->p.precision == MST_PREC_FP32)
+  if (pairs(c)) {
     CU(cudaMemcpyAsync(c->qf_old, c->qf_new, (size_t)c->dm.n_cells * sizeof(float4),
                        cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->ql_old, c->ql_new, (size_t)c->dm.n_cells * sizeof(float4),
+                       cudaMemcpyDeviceToDevice, c->stream));
+  }
   CU(cudaStreamSynchronize(c->stream));
   c->grad_valid = false;
   return MST_OK;
@@ -679,6 +776,10 @@ mst_status mst_get_face_flux(mst_ctx* c, double* f) {
   const int nF = c->dm.n_faces;
   if (!c->flux) {
     mst_status s = dalloc(c, &c->flux, (size_t)nF * 8 * sizeof(double));
+    if (s) return s;
+  }
+  if (pairs(c)) {
+    mst_status s = sync_double_from_pairs(c);
     if (s) return s;
   }
   if (c->p.order == 2 && !c->grad_valid) {
@@ -706,6 +807,10 @@ mst_status mst_get_face_flux(mst_ctx* c, double* f) {
 mst_status mst_get_gradient(mst_ctx* c, double* g) {
   if (!c || !g) return fail(MST_EINVAL, "NULL argument");
   if (c->p.order != 2) return fail(MST_EINVAL, "gradients exist for order 2 only");
+  if (pairs(c) && !c->grad_valid) {
+    mst_status s = sync_double_from_pairs(c);
+    if (s) return s;
+  }
   if (!c->grad_valid) {
     mst_status s = launch_grad(c, c->q_old);
     if (s) return s;
@@ -741,20 +846,37 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
     bool grad_ready = false;
     mst_status st = compute_dt(c, c->q_old, t_end, c->qf_old, &grad_ready);
     if (st) return st;
+    StageBufs b0;
+    b0.q = c->q_old;
+    b0.qf = c->qf_old;
+    b0.ql = c->ql_old;
     if (c->p.time_scheme == MST_TIME_EULER) {
-      st = run_stage(c, c->q_old, nullptr, c->q_new, 0, false, norms, false, c->qf_old,
-                     c->qf_new, grad_ready);
+      b0.qn = c->q_new;
+      b0.qfn = c->qf_new;
+      b0.qln = c->ql_new;
+      st = run_stage(c, b0, 0, false, norms, false, grad_ready);
     } else {
-      st = run_stage(c, c->q_old, nullptr, c->q_stage, 0, false, false, false, c->qf_old,
-                     c->qf_stage, grad_ready);
-      if (!st)
-        st = run_stage(c, c->q_stage, c->q_old, c->q_new, 1, false, norms, false,
-                       c->qf_stage, c->qf_new);
+      b0.qn = c->q_stage;
+      b0.qfn = c->qf_stage;
+      b0.qln = c->ql_stage;
+      st = run_stage(c, b0, 0, false, false, false, grad_ready);
+      StageBufs b1;
+      b1.q = c->q_stage;
+      b1.qf = c->qf_stage;
+      b1.ql = c->ql_stage;
+      b1.q0 = c->q_old;
+      b1.q0f = c->qf_old;
+      b1.q0l = c->ql_old;
+      b1.qn = c->q_new;
+      b1.qfn = c->qf_new;
+      b1.qln = c->ql_new;
+      if (!st) st = run_stage(c, b1, 1, false, norms, false);
     }
     if (st) return st;
     if (norms && (st = finalize_norms(c, true))) return st;
     std::swap(c->q_old, c->q_new);
     std::swap(c->qf_old, c->qf_new);
+    std::swap(c->ql_old, c->ql_new);
   }
   CU(cudaEventRecord(c->ev1, c->stream));
   c->timed = true;

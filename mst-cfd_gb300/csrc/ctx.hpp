@@ -25,6 +25,7 @@ struct DevArrays {
   float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr;
   double* c_vol = nullptr;
   double* c_ivol = nullptr;
+  float2* c_ivol_ff = nullptr;
   int *c_ptr = nullptr, *cf_face = nullptr, *cf_slot = nullptr, *cf_nb = nullptr,
       *cf_nb_fix = nullptr, *t_own_ptr = nullptr, *t_bor_ptr = nullptr,
       *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr;
@@ -40,7 +41,9 @@ struct mst_ctx {
   mst::DevMesh dm{};
   double4_32a *q_old = nullptr, *q_new = nullptr, *q_stage = nullptr,
               *r = nullptr, *stage_in = nullptr;
-  float4 *qf_old = nullptr, *qf_new = nullptr, *qf_stage = nullptr;  // FP32 copies
+  // FP32 path: state as float pairs, hi parts (qf_*) and lo parts (ql_*)
+  float4 *qf_old = nullptr, *qf_new = nullptr, *qf_stage = nullptr;
+  float4 *ql_old = nullptr, *ql_new = nullptr, *ql_stage = nullptr;
   void* grad = nullptr;
   double* flux = nullptr;      // [nF][8] debug output
   double* partials = nullptr;  // [max(nT, nBlocks)][kNormSlots]

@@ -21,6 +21,7 @@ struct DevMesh {
   const float2* f_r1_32;
   const double* c_vol;
   const double* c_ivol;  // 1/V (production paths; the exact path divides)
+  const float2* c_ivol_ff;  // 1/V as an unevaluated float pair (hi, lo)
   const int* c_ptr;
   const int* cf_face;
   const int* cf_slot;
@@ -40,6 +41,15 @@ struct StepArgs {
   const double4_32a* q;   // state the residual is evaluated on
   const float4* qf;       // its FP32 copy (FP32 path; nullptr: convert q)
   float4* qfn;            // FP32 copy of the updated state (or nullptr)
+  // FP32 path with the state as float pairs (value = hi + lo): qf/qfn are
+  // the hi parts, these the lo parts; q0f/q0lo = Q^n for the second stage.
+  // When qlo is nullptr the state is the FP64 q/q0/qn.
+  const float4* qlo;
+  float4* qlon;
+  const float4* q0f;
+  const float4* q0lo;
+  float dt_ff[2];         // fixed step as a float pair (mst_solve)
+  const float* dt_ff_dev; // step as a float pair on the device (or nullptr)
   const double4_32a* q0;  // Q^n for the second RK stage (else nullptr)
   double4_32a* qn;        // updated state
   const void* grad;       // [n_cells][2][4] in the path's precision

@@ -161,6 +161,20 @@ double om_spectral_dt(const om_mesh *m, const double *q, double cfl,
 int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
                 int nsteps, double t_end, double *time, om_norms *last);
 
+/* ------------------------------------------------------------------ */
+/* sparse sweeps of lusolver/ (mstoracle_lu.c)                          */
+/* ------------------------------------------------------------------ */
+/* Scalar SparseSolverNUM::solveILUSGS (gs = 0) or solveGS (gs = 1) on the
+ * system built by the ordered insertions (rows[i], cols[i], vals[i]) with
+ * ops[i] = 0 setELE, 1 addELE.  x: initial guess in, solution out. */
+int om_lu_scalar(int gs, int dim, int n, const int *rows, const int *cols,
+                 const int *ops, const double *vals, const double *b, double *x,
+                 int *iterations);
+/* Block SparseSolver<Matrix4d, Vector4d>::solveILU: vals [n][16] row-major
+ * blocks (diagonal entries setD, below setL, above setU), b and x [dim][4]. */
+int om_lu_block(int dim, int n, const int *rows, const int *cols,
+                const double *vals, const double *b, double *x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,9 @@ def lib():
         L.om_spectral_dt.restype = C.c_double
         L.om_step_ext.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParamsExt), _dp,
                                   C.c_int, C.c_double, _dp, C.POINTER(_ONorms)]
+        L.om_lu_scalar.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp, _dp, _dp,
+                                   _ip]
+        L.om_lu_block.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -285,3 +288,24 @@ def step_ext(mesh, prm, q, nsteps, t_end=0.0, time=0.0):
         raise RuntimeError("om_step_ext failed")
     return q, dict(linf_change=np.array(n.linf[:]), l2_resid=np.array(n.l2[:]),
                    mass=n.mass, dt=n.dt, time=t.value)
+
+
+# ---------------------------------------------------------------------------
+# lusolver sweeps
+# ---------------------------------------------------------------------------
+def lu_scalar(gs, dim, rows, cols, ops, vals, b, x0):
+    rows, cols, ops = (np.ascontiguousarray(a, dtype=np.int32) for a in (rows, cols, ops))
+    vals, b = _f64(vals), _f64(b)
+    x = _f64(x0).copy()
+    it = C.c_int()
+    lib().om_lu_scalar(int(gs), int(dim), len(rows), _i(rows), _i(cols), _i(ops), _d(vals),
+                       _d(b), _d(x), C.byref(it))
+    return x, it.value
+
+
+def lu_block(dim, rows, cols, vals, b, x0):
+    rows, cols = (np.ascontiguousarray(a, dtype=np.int32) for a in (rows, cols))
+    vals, b = _f64(vals), _f64(b)
+    x = _f64(x0).copy()
+    lib().om_lu_block(int(dim), len(rows), _i(rows), _i(cols), _d(vals), _d(b), _d(x))
+    return x
