@@ -205,7 +205,9 @@ typedef struct mst_norms {
  * serialised by the caller.  The first call on a device looks up the
  * array's device address; make that first call before any stream capture.
  * Runs on the context's stream and returns when the outputs are written;
- * the caller must have finished writing q_dev before the call. */
+ * the caller must have finished writing q_dev before the call.  On the FP32
+ * path the update is done in FP64 on the caller's buffers (mst_solve keeps
+ * that path's state as float pairs), so the two agree to FP32 rounding. */
 mst_status mst_solve_device_noalloc(mst_ctx *c, const double *q_dev,
                                    double *qnew_dev, double *r_dev,
                                    double *norms_dev);
@@ -223,6 +225,34 @@ mst_status mst_get_time(mst_ctx *c, double *t);
  * context's stream: elapsed milliseconds between its first and last
  * kernel, and the number of kernels launched. */
 mst_status mst_last_timing(mst_ctx *c, double *ms, int *launches);
+
+/* ------------------------------------------------------------------ */
+/* sparse LU-SGS / Gauss-Seidel sweeps (the reference's lusolver)      */
+/* ------------------------------------------------------------------ */
+typedef struct mst_lu mst_lu;
+enum { MST_LU_ILUSGS = 0, MST_LU_GS = 1 };
+
+/* A sparse system given as the ordered insertions the reference's solvers
+ * receive: block = 1 replaces SparseSolverNUM built with setELE (ops[i] =
+ * 0) / addELE (ops[i] = 1) (lusolver/SparseSolverNUM.cpp:115-140); block =
+ * 4 replaces SparseSolver<Matrix4d, Vector4d> built with setD/setL/setU
+ * (lusolver/SparseSolver.cpp:35-48), vals then holding row-major 4x4 blocks
+ * (ops may be NULL).  Duplicates are kept, as in the reference.  Rows are
+ * grouped into dependency levels for the GPU sweeps. */
+mst_status mst_lu_create(int block, int dim, int n, const int *rows,
+                         const int *cols, const int *ops, const double *vals,
+                         mst_lu **out);
+/* SparseSolverNUM::solveILUSGS (SparseSolverNUM.cpp:144-212) or solveGS
+ * (:214-252) for block = 1; SparseSolver::solveILU (SparseSolver.cpp:53-104)
+ * for block = 4.  x holds the initial guess and receives the solution;
+ * iterations (nullable) receives the outer iterations run (at most
+ * LU_INTERVAL = 5, fewer when the reference's exit test triggers).  Results
+ * are bit-identical to the reference's. */
+mst_status mst_lu_solve(mst_lu *s, int method, const double *b, double *x,
+                        int *iterations);
+/* Number of dependency levels of the forward and backward sweeps. */
+mst_status mst_lu_levels(const mst_lu *s, int *forward, int *backward);
+mst_status mst_lu_destroy(mst_lu *s);
 
 /* Per-kernel CUDA-event timing on the context's stream.  When enabled,
  * every kernel launch of mst_solve/mst_step is bracketed by events; the

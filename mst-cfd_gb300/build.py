@@ -7,6 +7,7 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/kernels_fast.cu   FP64/FP32 production kernels (FMA allowed)
   * csrc/capi.cu           the C ABI of include/mstcfd.h
   * csrc/noalloc.cu        the allocation-free solve entry point
+  * csrc/lusgs.cu          level-scheduled LU-SGS / GS sweeps, --fmad=false
 """
 import os
 import shutil
@@ -47,6 +48,7 @@ def _units():
                                             os.path.join(CSRC, "kernels_fast.cu")]),
         ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
         ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
+        ("lusgs.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "lusgs.cu")]),
     ]
 
 

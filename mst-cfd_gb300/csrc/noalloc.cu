@@ -10,6 +10,10 @@
 // at set-up (that call allocates the resident mesh), then calls this entry
 // point as often as it likes with its own input and output buffers.
 //
+// Arithmetic: the context's precision; the state is the caller's FP64
+// buffers, so on the FP32 path the update is done in FP64 (mst_solve keeps
+// that path's state as float pairs) and the two agree to FP32 rounding.
+//
 // Scratch: the gradient and the per-tile norm partials that mst_solve keeps
 // in context allocations live here in one file-scope device array of fixed
 // size instead, so a mesh may have at most kMaxCells cells.  Every GPU that

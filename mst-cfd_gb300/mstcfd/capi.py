@@ -16,6 +16,7 @@ OK, EINVAL, EMESH, ECUDA, EDIVERGED, ETIMEOUT, ENOMEM, EUNSUPPORTED = range(8)
 FLUX_AUSM, FLUX_ROE = 0, 1
 LIMITER_NONE, LIMITER_MINMOD, LIMITER_VANLEER, LIMITER_VANALBADA = range(4)
 PREC_FP64_EXACT, PREC_FP64, PREC_FP32 = range(3)
+LU_ILUSGS, LU_GS = range(2)
 TIME_EULER, TIME_RK2 = range(2)
 DT_FIXED, DT_CFL_GLOBAL, DT_CFL_LOCAL = range(3)
 
@@ -119,6 +120,11 @@ def load():
         "mst_set_device": (C.c_int, [C.c_int]),
         "mst_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p]),
+        "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
+                                    C.POINTER(C.c_void_p)]),
+        "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),
+        "mst_lu_levels": (C.c_int, [C.c_void_p, _ip, _ip]),
+        "mst_lu_destroy": (C.c_int, [C.c_void_p]),
         "mst_last_error": (C.c_char_p, []),
         "mst_abi_version": (C.c_int, []),
     }

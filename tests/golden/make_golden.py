@@ -12,6 +12,10 @@ from its own sources into oracle/_ref (oracle/ref/build_ref.sh):
   * five steps of the reference's own time loop (Time::goNextTimeStep with
     its Sod initialisation and DT = 1/4000) and the L-infinity residual rows
     it logs.
+and lusolver.npz: sparse systems with a mesh's sparsity, inserted in a
+shuffled order (setELE/addELE mixed, duplicates kept), solved by the
+reference's SparseSolverNUM::solveILUSGS / solveGS and
+SparseSolver<Matrix4d, Vector4d>::solveILU (oracle/ref/harness_lu.cpp).
 The GPU tests compare the CUDA path against these arrays bit-for-bit on
 machines where the reference is absent.
 
@@ -77,7 +81,56 @@ def make(name, mesh):
     return path
 
 
+def lu_system(dim_mesh, block, diag_scale, seed):
+    """A sparse system with the sparsity of a triangle mesh's cell adjacency,
+    inserted in a shuffled order with setELE/addELE mixed and some
+    duplicated entries (the reference keeps duplicates)."""
+    rng = np.random.default_rng(seed)
+    m = mg.tri_box(*dim_mesh, seed=seed)
+    fc = m["face_cells"]
+    fc = fc[fc[:, 1] >= 0]
+    dim = int(m["n_cells"])
+    ins = [(int(a), int(b)) for a, b in fc] + [(int(b), int(a)) for a, b in fc]
+    ins += [(i, i) for i in range(dim)]
+    ins += [(i, i) for i in rng.choice(dim, dim // 5, replace=False)]  # repeated diagonal
+    ins += [ins[i] for i in rng.choice(len(fc), len(fc) // 10, replace=False)]  # duplicates
+    order = rng.permutation(len(ins))
+    rows = np.array([ins[i][0] for i in order], np.int32)
+    cols = np.array([ins[i][1] for i in order], np.int32)
+    ops = rng.integers(0, 2, len(rows)).astype(np.int32)
+    B = 16 if block else 1
+    vals = rng.uniform(-1, 1, (len(rows), B))
+    diag = rows == cols
+    if block:
+        eye = np.eye(4).ravel()
+        vals[diag] = diag_scale * eye * rng.uniform(1, 1.5, (diag.sum(), 1)) + 0.2 * vals[diag]
+    else:
+        vals[diag, 0] = diag_scale * rng.uniform(1, 1.5, diag.sum())
+    nb = 4 if block else 1
+    b = rng.uniform(1, 2, dim * nb)
+    x0 = rng.uniform(0.5, 1.5, dim * nb)
+    return dim, rows, cols, ops, vals.ravel(), b, x0
+
+
+def make_lu():
+    out = {}
+    specs = [("ilusgs", 0, (16, 10), False, 7.0, 31), ("ilusgs_fast", 0, (12, 8), False, 60.0, 32),
+             ("gs", 1, (16, 10), False, 9.0, 33), ("gs_fast", 1, (12, 8), False, 80.0, 34),
+             ("block", 2, (10, 8), True, 8.0, 35)]
+    for name, mode, dm, block, ds, seed in specs:
+        dim, rows, cols, ops, vals, b, x0 = lu_system(dm, block, ds, seed)
+        x = refrun.run_lu(mode, dim, rows, cols, ops, vals, b, x0)
+        for k, v in dict(dim=np.array(dim), mode=np.array(mode), rows=rows, cols=cols,
+                         ops=ops, vals=vals, b=b, x0=x0, x=x).items():
+            out[f"{name}_{k}"] = v
+    path = os.path.join(OUT, "lusolver.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 if __name__ == "__main__":
     for name, mesh in cases():
         p = make(name, mesh)
         print(p, os.path.getsize(p))
+    p = make_lu()
+    print(p, os.path.getsize(p))

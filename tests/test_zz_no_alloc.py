@@ -6,9 +6,13 @@ The test plays such a caller: it owns its device buffers (allocated here
 through the CUDA runtime), calls the new entry point through the C ABI twice
 in a row on the same buffers, and checks each call's new state, residual and
 norms against the existing entry points (mst_solve / mst_step) on the same
-input.  Tolerance: the same kernels run in both, so states and residuals
-must be identical; the L2 norms are compared to rtol 1e-12 and the mass to
-rtol 1e-13 as elsewhere in the GPU tests.  Kept in its own file, collected
+input.  Tolerance: in FP64_EXACT the same kernels run in both, so states
+and residuals must be identical (L2 norms to rtol 1e-12, mass to rtol 1e-13
+as elsewhere in the GPU tests).  On the FP32 path mst_solve keeps the state
+as float pairs while this entry point updates the caller's FP64 buffers, so
+the two agree to FP32 rounding: the FP32 tolerances of the other tests
+(residual within 2e-5 of its largest value per component, states within
+1e-6 of theirs, norms to rtol 1e-5).  Kept in its own file, collected
 last, so a run that stops at the first failure has run every other test.
 """
 import ctypes as C
@@ -98,11 +102,20 @@ def test_noalloc_matches_existing_entry_points(order, prec):
             qn = bqn.get((nC, 4))[perm]
             r = br.get((nC, 4))[perm]
             nrm = bn.get(10)
-            assert np.array_equal(qn, want_qn), call
-            assert np.array_equal(r, want_r), call
-            assert np.array_equal(nrm[:4], want_norms["linf_change"]), call
-            assert np.allclose(nrm[4:8], want_norms["l2_resid"], rtol=1e-12, atol=0), call
-            assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-13, atol=0), call
+            if prec == 0:
+                assert np.array_equal(qn, want_qn), call
+                assert np.array_equal(r, want_r), call
+                assert np.array_equal(nrm[:4], want_norms["linf_change"]), call
+                assert np.allclose(nrm[4:8], want_norms["l2_resid"], rtol=1e-12, atol=0), call
+                assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-13, atol=0), call
+            else:
+                scale = np.abs(want_r).max(0)
+                assert np.all(np.abs(r - want_r).max(0) <= 2e-5 * scale), call
+                assert np.all(np.abs(qn - want_qn) <= 1e-6 * np.abs(want_qn).max(0)), call
+                assert np.allclose(nrm[:8], np.concatenate([want_norms["linf_change"],
+                                                             want_norms["l2_resid"]]),
+                                   rtol=1e-5, atol=0), call
+                assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-12, atol=0), call
             assert nrm[9] == want_norms["dt"], call
     finally:
         for b in (bq, bqn, br, bn):
