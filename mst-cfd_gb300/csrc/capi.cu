@@ -65,6 +65,13 @@ __global__ void k_to_pairs(const double4_32a* __restrict__ q, float4* __restrict
   lo[i] = make_float4((float)(v.x - (double)h.x), (float)(v.y - (double)h.y),
                       (float)(v.z - (double)h.z), (float)(v.w - (double)h.w));
 }
+__global__ void k_to_pairs1(const double* __restrict__ v, float2* __restrict__ out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float h = (float)v[i];
+  out[i] = make_float2(h, (float)(v[i] - (double)h));
+}
+
 // pairs -> double, gathered through idx (idx = nullptr: same order)
 __global__ void k_from_pairs(const float4* __restrict__ hi, const float4* __restrict__ lo,
                              const int* __restrict__ idx, double4_32a* __restrict__ q, int n) {
@@ -229,16 +236,19 @@ void drain_profile(mst_ctx* c) {
 // gradient of q (qf: its FP32 copy on the FP32 path); with dt_part it also
 // writes the CFL step partials (and dt_cell)
 mst_status launch_grad(mst_ctx* c, const double4_32a* q, const float4* qf = nullptr,
-                       double* dt_part = nullptr, double* dt_cell = nullptr) {
+                       double* dt_part = nullptr, bool local_dt = false) {
   ProfScope ps(c, c->p.precision == MST_PREC_FP32 ? "k_gradient<f32>" : "k_gradient<f64>");
-  if (c->p.precision != MST_PREC_FP32) qf = nullptr;
+  const bool f32 = c->p.precision == MST_PREC_FP32;
+  if (!f32) qf = nullptr;
+  double* dt_cell = (local_dt && !f32) ? c->dt_cell : nullptr;
+  float2* dt_cell_ff = (local_dt && f32) ? c->dt_cell_ff : nullptr;
   cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                       ? mst::exact::launch_gradient_dt(prec_of(c->p), c->dm, q, qf, c->grad,
                                                        c->p.reference_quirks, c->p.cfl,
-                                                       dt_cell, dt_part, c->stream)
+                                                       dt_cell, dt_cell_ff, dt_part, c->stream)
                       : mst::fast::launch_gradient_dt(prec_of(c->p), c->dm, q, qf, c->grad,
                                                       c->p.reference_quirks, c->p.cfl,
-                                                      dt_cell, dt_part, c->stream);
+                                                      dt_cell, dt_cell_ff, dt_part, c->stream);
   c->last_launches++;
   if (e != cudaSuccess) return fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
   c->grad_valid = true;
@@ -327,7 +337,10 @@ mst_status run_stage(mst_ctx* c, const StageBufs& b, int stage, bool fixed_dt, b
   a.r_out = keep_residual ? c->r : nullptr;
   a.stage = stage;
   if (!fixed_dt) {
-    if (c->p.dt_mode == MST_DT_CFL_LOCAL) a.dt_cell = c->dt_cell;
+    if (c->p.dt_mode == MST_DT_CFL_LOCAL) {
+      a.dt_cell = c->dt_cell;
+      if (pairs(c)) a.dt_cell_ff = c->dt_cell_ff;
+    }
     else a.dt_dev = c->scal;
   }
   a.partials = norms ? c->partials : nullptr;
@@ -342,8 +355,7 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end,
   const int nC = c->dm.n_cells;
   int mode = 0;
   if (c->p.dt_mode != MST_DT_FIXED && c->p.order == 2 && grad_ready) {
-    mst_status st = launch_grad(c, q, qf, c->dt_part,
-                                c->p.dt_mode == MST_DT_CFL_LOCAL ? c->dt_cell : nullptr);
+    mst_status st = launch_grad(c, q, qf, c->dt_part, c->p.dt_mode == MST_DT_CFL_LOCAL);
     if (st) return st;
     *grad_ready = true;
     mode = 1;
@@ -356,6 +368,10 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end,
                                                         c->dt_cell, c->dt_part, c->stream);
     c->last_launches++;
     if (e != cudaSuccess) return fail(MST_ECUDA, std::string("spectral_dt: ") + cudaGetErrorString(e));
+    if (pairs(c) && c->p.dt_mode == MST_DT_CFL_LOCAL) {
+      k_to_pairs1<<<(nC + 255) / 256, 256, 0, c->stream>>>(c->dt_cell, c->dt_cell_ff, nC);
+      CU(cudaGetLastError());
+    }
     mode = 1;
   }
   ProfScope ps(c, "k_finalize_dt");
@@ -639,6 +655,7 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
                    std::max<size_t>(L.n_tiles, nB) * kNormSlots * sizeof(double))) ||
       (st = dalloc(c.get(), &c->dt_part, nB * sizeof(double))) ||
       (st = dalloc(c.get(), &c->dt_cell, nC * sizeof(double))) ||
+      (st = dalloc(c.get(), &c->dt_cell_ff, nC * sizeof(float2))) ||
       (st = dalloc(c.get(), &c->scal, 4 * sizeof(double))) ||
       (st = dalloc(c.get(), &c->norms, (kNormSlots + 2) * sizeof(double))))
     return st;

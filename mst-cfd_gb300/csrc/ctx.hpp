@@ -49,6 +49,7 @@ struct mst_ctx {
   double* partials = nullptr;  // [max(nT, nBlocks)][kNormSlots]
   double* dt_part = nullptr;   // [nBlocks]
   double* dt_cell = nullptr;   // [nC]
+  float2* dt_cell_ff = nullptr;  // [nC] local steps as float pairs (FP32 path)
   double* scal = nullptr;      // [0] dt, [1] time
   double* norms = nullptr;     // [kNormSlots + 2]
   int last_launches = 0;

@@ -49,6 +49,7 @@ struct StepArgs {
   const float4* q0f;
   const float4* q0lo;
   float dt_ff[2];         // fixed step as a float pair (mst_solve)
+  const float2* dt_cell_ff;  // local step per cell as float pairs (FP32 path)
   const float* dt_ff_dev; // step as a float pair on the device (or nullptr)
   const double4_32a* q0;  // Q^n for the second RK stage (else nullptr)
   double4_32a* qn;        // updated state
@@ -77,8 +78,8 @@ enum { kFluxAusm = 0, kFluxRoe = 1 };
   cudaError_t launch_gradient_dt(int prec, const DevMesh& m,                  \
                                  const double4_32a* q, const float4* qf,      \
                                  void* grad, int quirks, double cfl,          \
-                                 double* dt_cell, double* dt_part,            \
-                                 cudaStream_t s);                             \
+                                 double* dt_cell, float2* dt_cell_ff,         \
+                                 double* dt_part, cudaStream_t s);            \
   cudaError_t launch_to_f32(const double4_32a* q, float4* qf, int n,         \
                             cudaStream_t s);                                  \
   cudaError_t launch_flux_update(int prec, int flux, int order,              \

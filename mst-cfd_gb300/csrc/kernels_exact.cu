@@ -11,12 +11,12 @@ constexpr bool kExactArith = true;
 
 cudaError_t launch_gradient(int, const DevMesh& m, const double4_32a* q,
                             void* grad, int quirks, cudaStream_t s) {
-  return gradient_t<double>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, s);
+  return gradient_t<double>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, nullptr, s);
 }
 cudaError_t launch_gradient_dt(int, const DevMesh& m, const double4_32a* q,
                                const float4*, void* grad, int quirks, double cfl,
-                               double* dt_cell, double* dt_part, cudaStream_t s) {
-  return gradient_t<double>(m, q, nullptr, grad, quirks, cfl, dt_cell, dt_part, s);
+                               double* dt_cell, float2*, double* dt_part, cudaStream_t s) {
+  return gradient_t<double>(m, q, nullptr, grad, quirks, cfl, dt_cell, nullptr, dt_part, s);
 }
 cudaError_t launch_to_f32(const double4_32a* q, float4* qf, int n, cudaStream_t s) {
   k_to_f32<<<(n + 255) / 256, 256, 0, s>>>(q, qf, n);

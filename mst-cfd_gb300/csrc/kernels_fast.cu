@@ -12,15 +12,16 @@ constexpr bool kExactArith = false;
 cudaError_t launch_gradient(int prec, const DevMesh& m, const double4_32a* q,
                             void* grad, int quirks, cudaStream_t s) {
   if (prec == kPrecF32)
-    return gradient_t<float>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, s);
-  return gradient_t<double>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, s);
+    return gradient_t<float>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, nullptr, s);
+  return gradient_t<double>(m, q, nullptr, grad, quirks, 0.0, nullptr, nullptr, nullptr, s);
 }
 cudaError_t launch_gradient_dt(int prec, const DevMesh& m, const double4_32a* q,
                                const float4* qf, void* grad, int quirks, double cfl,
-                               double* dt_cell, double* dt_part, cudaStream_t s) {
+                               double* dt_cell, float2* dt_cell_ff, double* dt_part,
+                               cudaStream_t s) {
   if (prec == kPrecF32)
-    return gradient_t<float>(m, q, qf, grad, quirks, cfl, dt_cell, dt_part, s);
-  return gradient_t<double>(m, q, nullptr, grad, quirks, cfl, dt_cell, dt_part, s);
+    return gradient_t<float>(m, q, qf, grad, quirks, cfl, dt_cell, dt_cell_ff, dt_part, s);
+  return gradient_t<double>(m, q, nullptr, grad, quirks, cfl, dt_cell, nullptr, dt_part, s);
 }
 cudaError_t launch_to_f32(const double4_32a* q, float4* qf, int n, cudaStream_t s) {
   k_to_f32<<<(n + 255) / 256, 256, 0, s>>>(q, qf, n);
