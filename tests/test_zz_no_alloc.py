@@ -12,7 +12,8 @@ as elsewhere in the GPU tests).  On the FP32 path mst_solve keeps the state
 as float pairs while this entry point updates the caller's FP64 buffers, so
 the two agree to FP32 rounding: the FP32 tolerances of the other tests
 (residual within 2e-5 of its largest value per component, states within
-1e-6 of theirs, norms to rtol 1e-5).  Kept in its own file, collected
+1e-6 of theirs, norms to rtol 1e-5, and the mass to rtol 1e-9, since the
+inlet and outlet fluxes that change it carry FP32 rounding).  Kept in its own file, collected
 last, so a run that stops at the first failure has run every other test.
 """
 import ctypes as C
@@ -115,7 +116,7 @@ def test_noalloc_matches_existing_entry_points(order, prec):
                 assert np.allclose(nrm[:8], np.concatenate([want_norms["linf_change"],
                                                              want_norms["l2_resid"]]),
                                    rtol=1e-5, atol=0), call
-                assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-12, atol=0), call
+                assert np.isclose(nrm[8], want_norms["mass"], rtol=1e-9, atol=0), call
             assert nrm[9] == want_norms["dt"], call
     finally:
         for b in (bq, bqn, br, bn):
