@@ -72,11 +72,18 @@ typedef struct mst_params {
    * symmetry = mirrored reconstructed state, 2nd-order outlet =
    * reconstructed zero-gradient). */
   int reference_quirks;
-  int reserved[7];
+  /* Laminar viscous term (order 2 only; the reference's updateViscid,
+   * RhoSolver.cpp:371-429, restated with its defects corrected): stress
+   * tau = mu (grad u + grad u^T) + lambda (div u) I, heat flux kappa grad T
+   * with T = e / cv; walls become no-slip and adiabatic.  Defaults are
+   * CONST.h's VISCIDMU, VISCIDLAMBDA, TEMPK and CV. */
+  int viscous;
+  double mu, lambda, kappa, cv;
+  int reserved[6];
 } mst_params;
 
 /* Reference defaults: AUSM+, 1st order, FP64_EXACT, Euler, DT = 1/4000,
- * inlet state of CONST.h, quirks on. */
+ * inlet state of CONST.h, quirks on, inviscid. */
 void mst_params_default(mst_params *p);
 
 /* ------------------------------------------------------------------ */

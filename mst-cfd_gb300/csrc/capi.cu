@@ -175,6 +175,10 @@ mst_status check_params(const mst_params* p) {
     return fail(MST_EINVAL, "dt must be >= 0");
   if (p->dt_mode != MST_DT_FIXED && !(p->cfl > 0))
     return fail(MST_EINVAL, "cfl must be > 0");
+  if (p->viscous && p->order != 2)
+    return fail(MST_EINVAL, "the viscous term needs order 2 (cell gradients)");
+  if (p->viscous && !(p->mu >= 0 && p->kappa >= 0 && p->cv > 0))
+    return fail(MST_EINVAL, "bad viscous coefficients");
   return MST_OK;
 }
 
@@ -295,6 +299,11 @@ mst::StepArgs base_args(mst_ctx* c) {
   a.quirks = c->p.reference_quirks;
   a.limiter = c->p.limiter;
   for (int k = 0; k < 4; ++k) a.inlet[k] = c->p.inlet_q[k];
+  a.viscous = c->p.viscous;
+  a.mu = c->p.mu;
+  a.lam = c->p.lambda;
+  a.kappa = c->p.kappa;
+  a.cv = c->p.cv;
   return a;
 }
 
@@ -457,6 +466,11 @@ void mst_params_default(mst_params* p) {
   p->inlet_q[2] = 1.0 * 0;
   p->inlet_q[3] = 1 * (1 / 286.32 * 715.8 + 0.5 * (0 * 0 + 0 * 0));
   p->reference_quirks = 1;
+  p->viscous = 0;
+  p->mu = 1.7894e-05;              // VISCIDMU (CONST.h:46)
+  p->lambda = -0.666667 * 1.7894e-05;  // VISCIDLAMBDA (CONST.h:47)
+  p->kappa = 0.0242;               // TEMPK (CONST.h:48)
+  p->cv = 715.8;                   // CV (CONST.h:39)
 }
 
 mst_status mst_mesh_read_msh(const char* path, mst_mesh** out) {
@@ -592,6 +606,16 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
     CU(up(&d.f_r0_32, as_f2(L.f_r0)));
     CU(up(&d.f_r1_32, as_f2(L.f_r1)));
     CU(up(&d.cf_w32, as_f2(L.cf_w)));
+    {
+      std::vector<double> fe(L.n_faces);
+      std::vector<float> fe32(L.n_faces);
+      for (int i = 0; i < L.n_faces; ++i) {
+        fe[i] = m->host.face_eta0[L.face_iperm[i]];
+        fe32[i] = (float)fe[i];
+      }
+      CU(up(&d.f_eta, fe));
+      CU(up(&d.f_eta32, fe32));
+    }
     CU(up(&d.c_vol, L.c_vol));
     std::vector<double> ivol(L.c_vol.size());
     for (size_t i = 0; i < ivol.size(); ++i) ivol[i] = 1.0 / L.c_vol[i];
@@ -626,6 +650,8 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.f_dir32 = d.f_dir32;
   dm.f_r0_32 = d.f_r0_32;
   dm.f_r1_32 = d.f_r1_32;
+  dm.f_eta = d.f_eta;
+  dm.f_eta32 = d.f_eta32;
   dm.c_vol = d.c_vol;
   dm.c_ivol = d.c_ivol;
   dm.c_ivol_ff = d.c_ivol_ff;

@@ -23,6 +23,8 @@ struct DevArrays {
   int* f_info = nullptr;
   double2 *f_dir = nullptr, *f_r0 = nullptr, *f_r1 = nullptr, *cf_w = nullptr;
   float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr;
+  double* f_eta = nullptr;
+  float* f_eta32 = nullptr;
   double* c_vol = nullptr;
   double* c_ivol = nullptr;
   float2* c_ivol_ff = nullptr;

@@ -19,6 +19,8 @@ struct DevMesh {
   const float2* f_dir32;
   const float2* f_r0_32;
   const float2* f_r1_32;
+  const double* f_eta;    // eta0 per face (viscous face interpolation)
+  const float* f_eta32;
   const double* c_vol;
   const double* c_ivol;  // 1/V (production paths; the exact path divides)
   const float2* c_ivol_ff;  // 1/V as an unevaluated float pair (hi, lo)
@@ -62,6 +64,8 @@ struct StepArgs {
   int quirks;             // reproduce the reference's quirks
   int limiter;            // MST_LIMITER_*
   double inlet[4];
+  int viscous;            // laminar viscous term on
+  double mu, lam, kappa, cv;
   double* partials;       // [n_tiles][kNormSlots] or nullptr
 };
 

@@ -30,7 +30,8 @@ class Params(C.Structure):
                 ("precision", C.c_int), ("time_scheme", C.c_int),
                 ("dt_mode", C.c_int), ("dt", C.c_double), ("cfl", C.c_double),
                 ("inlet_q", C.c_double * 4), ("reference_quirks", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("viscous", C.c_int), ("mu", C.c_double), ("lambda_", C.c_double),
+                ("kappa", C.c_double), ("cv", C.c_double), ("reserved", C.c_int * 6)]
 
 
 class MeshDesc(C.Structure):

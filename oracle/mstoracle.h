@@ -141,6 +141,8 @@ typedef struct om_params_ext {
   int dt_mode;      /* OM_DT_* */
   double dt, cfl;
   double inlet_q[4];
+  int viscous;      /* laminar viscous term (order 2) */
+  double mu, lam, kappa, cv;
 } om_params_ext;
 
 typedef struct om_norms {

@@ -18,6 +18,44 @@ void om_default_params_ext(om_params_ext *p) {
   p->dt = 1.0 / 4e+3;
   p->cfl = 0.5;
   om_reference_inlet(p->inlet_q);
+  p->viscous = 0;
+  p->mu = 1.7894e-05;
+  p->lam = -0.666667 * 1.7894e-05;
+  p->kappa = 0.0242;
+  p->cv = 715.8;
+}
+
+/* Laminar viscous term, the intent of RhoSolver::updateViscid
+ * (RhoSolver.cpp:371-429) with its defects corrected: primitive gradients
+ * from the conserved cell gradients by the chain rule, eta0-weighted face
+ * values and gradients, tau = mu (grad u + grad u^T) + lambda (div u) I,
+ * energy u.tau + kappa grad T (T = e / cv); no-slip adiabatic walls with the
+ * velocity gradient corrected along the cell-to-face vector. */
+static void prim_grad_e(const double q[4], const double g[8], double cv, double gu[2],
+                        double gv[2], double gT[2]) {
+  const double rho = q[0], u = q[1] / rho, v = q[2] / rho, er = q[3] / rho;
+  for (int d = 0; d < 2; ++d) {
+    gu[d] = (g[4 * d + 1] - u * g[4 * d]) / rho;
+    gv[d] = (g[4 * d + 2] - v * g[4 * d]) / rho;
+    const double ge = (g[4 * d + 3] - er * g[4 * d]) / rho - u * gu[d] - v * gv[d];
+    gT[d] = ge / cv;
+  }
+}
+static void sub_viscous_e(double u, double v, const double gu[2], const double gv[2],
+                          const double gT[2], double mu, double lam, double kappa, int heat,
+                          double F[8]) {
+  const double div = gu[0] + gv[1];
+  const double txx = mu * (2.0 * gu[0]) + lam * div;
+  const double tyy = mu * (2.0 * gv[1]) + lam * div;
+  const double txy = mu * (gu[1] + gv[0]);
+  const double qx = heat ? kappa * gT[0] : 0.0;
+  const double qy = heat ? kappa * gT[1] : 0.0;
+  F[1] = F[1] - txx;
+  F[2] = F[2] - txy;
+  F[3] = F[3] - ((u * txx + v * txy) + qx);
+  F[5] = F[5] - txy;
+  F[6] = F[6] - tyy;
+  F[7] = F[7] - ((u * txy + v * tyy) + qy);
 }
 
 static double shift(const om_mesh *m, int f, int d) {
@@ -151,6 +189,11 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
           memcpy(R, p->inlet_q, 32);
         } else if (type == 5) {
           memcpy(R, L, 32);
+        } else if (type == 3 && second && p->viscous) {
+          R[0] = L[0];
+          R[1] = -L[1];
+          R[2] = -L[2];
+          R[3] = L[3];
         } else if (type == 7 && second && p->quirks && !limited) {
           double rc[4], mm[4];
           recon_e(q0, grad + 8 * c0, r0x, r0y, rc);
@@ -166,6 +209,34 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
       for (int d = 0; d < 2; ++d) {
         if (flag[d]) fl(L, R, d, Fi + 4 * d);
         else fl(R, L, d, Fi + 4 * d);
+      }
+      if (second && p->viscous && (type == 2 || type == 3)) {
+        double gu[2], gv[2], gT[2];
+        prim_grad_e(q0, grad + 8 * c0, p->cv, gu, gv, gT);
+        if (type == 2) {
+          const double *q1 = q + 4 * c1;
+          const double eta = m->face_eta0[i], ome = 1.0 - eta;
+          double gu1[2], gv1[2], gT1[2], qf[4];
+          prim_grad_e(q1, grad + 8 * c1, p->cv, gu1, gv1, gT1);
+          for (int d = 0; d < 2; ++d) {
+            gu[d] = eta * gu[d] + ome * gu1[d];
+            gv[d] = eta * gv[d] + ome * gv1[d];
+            gT[d] = eta * gT[d] + ome * gT1[d];
+          }
+          for (int k = 0; k < 4; ++k) qf[k] = eta * q0[k] + ome * q1[k];
+          sub_viscous_e(qf[1] / qf[0], qf[2] / qf[0], gu, gv, gT, p->mu, p->lam, p->kappa, 1, Fi);
+        } else {
+          const double rl = sqrt(r0x * r0x + r0y * r0y);
+          const double ex = r0x / rl, ey = r0y / rl;
+          const double u0 = q0[1] / q0[0], v0 = q0[2] / q0[0];
+          const double cu = (0.0 - u0) / rl - (gu[0] * ex + gu[1] * ey);
+          const double cvv = (0.0 - v0) / rl - (gv[0] * ex + gv[1] * ey);
+          gu[0] = gu[0] + cu * ex;
+          gu[1] = gu[1] + cu * ey;
+          gv[0] = gv[0] + cvv * ex;
+          gv[1] = gv[1] + cvv * ey;
+          sub_viscous_e(0.0, 0.0, gu, gv, gT, p->mu, p->lam, p->kappa, 0, Fi);
+        }
       }
     }
   }

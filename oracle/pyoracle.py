@@ -42,7 +42,8 @@ class _OParamsExt(C.Structure):
     _fields_ = [("flux", C.c_int), ("order", C.c_int), ("limiter", C.c_int),
                 ("quirks", C.c_int), ("rk2", C.c_int), ("dt_mode", C.c_int),
                 ("dt", C.c_double), ("cfl", C.c_double),
-                ("inlet_q", C.c_double * 4)]
+                ("inlet_q", C.c_double * 4), ("viscous", C.c_int), ("mu", C.c_double),
+                ("lam", C.c_double), ("kappa", C.c_double), ("cv", C.c_double)]
 
 
 class _ONorms(C.Structure):
@@ -244,11 +245,16 @@ DT_FIXED, DT_CFL_GLOBAL, DT_CFL_LOCAL = range(3)
 
 
 def params_ext(flux=AUSM, order=1, limiter=0, quirks=1, rk2=0, dt_mode=0,
-               dt=1.0 / 4e3, cfl=0.5, inlet_q=None):
+               dt=1.0 / 4e3, cfl=0.5, inlet_q=None, viscous=0, mu=None, lam=None,
+               kappa=None, cv=None):
     p = _OParamsExt()
     lib().om_default_params_ext(C.byref(p))
     p.flux, p.order, p.limiter, p.quirks, p.rk2 = flux, order, limiter, quirks, rk2
     p.dt_mode, p.dt, p.cfl = dt_mode, float(dt), float(cfl)
+    p.viscous = int(viscous)
+    for k, v in (("mu", mu), ("lam", lam), ("kappa", kappa), ("cv", cv)):
+        if v is not None:
+            setattr(p, k, float(v))
     if inlet_q is not None:
         for k in range(4):
             p.inlet_q[k] = float(inlet_q[k])
