@@ -234,6 +234,55 @@ mst_status mst_get_time(mst_ctx *c, double *t);
 mst_status mst_last_timing(mst_ctx *c, double *ms, int *launches);
 
 /* ------------------------------------------------------------------ */
+/* result writer and checkpoint files                                  */
+/* ------------------------------------------------------------------ */
+/* Node averages of the current state, computed on the device as
+ * Work::writedataRhoBasedMshNodePlt does (work/Work.cpp:240-300): face
+ * values (eta0 blend on type-2 faces, the cell value on boundary faces),
+ * averaged onto each node over its faces with weights 1/area.  With
+ * reference_quirks the weight of every face of node i is 1/area of face i
+ * (Work.cpp:292-293 index faces by the node id; the call then needs
+ * n_nodes <= n_faces); without, each face's own 1/area.
+ * node_q [n_nodes][4] conserved, node_vars [n_nodes][6] = rho, u, v, T, p,
+ * Ma (work/FUNCTION.cpp:8-20, cv from the parameters); nodes in file
+ * order; either may be NULL. */
+mst_status mst_node_values(mst_ctx *c, double *node_q, double *node_vars);
+
+/* Tecplot ASCII file of the current state: the format of
+ * Work::writedataRhoBasedMshNodePlt (Work.cpp:204-319), zone title zone_t,
+ * one POINT row X Y rho u v T p Ma per node ("%.15f", space-terminated),
+ * then 1-based node lists per cell in the reader's node order
+ * (mesh/MshBlock.cpp:335-367).  With reference_quirks the file is
+ * byte-identical to the reference's (its stray title quote, zone type
+ * FEQUADRILATERAL for every mesh, 3 ids for triangles, quads in the
+ * reader's node order, which is a bow tie); without, the title is well
+ * formed, all-triangle meshes are FETRIANGLE zones, quads are written in
+ * cyclic order (0 1 3 2 of the reader's) and triangles in mixed zones
+ * repeat their last node. */
+mst_status mst_write_plt(mst_ctx *c, const char *path, int zone_t);
+
+/* Text checkpoint of the current state: one line per cell (file order) of
+ * 4 "%.15f" numbers, each followed by a space, the format of
+ * Work::writedataCellContinue (Work.cpp:483-514).  Not exact: 15
+ * decimals. */
+mst_status mst_write_cell_text(mst_ctx *c, const char *path);
+/* Reads such a file into the state, as Work::readPbasedCellPlt
+ * (Work.cpp:432-482) does: the first 4 space-separated numbers of each
+ * line.  MST_EINVAL (and the state unchanged) on a missing file, too few
+ * lines or too few numbers on a line. */
+mst_status mst_read_cell_text(mst_ctx *c, const char *path);
+
+/* Exact binary checkpoint: the FP64 state, on the FP32 path also the
+ * float-pair parts, the time and the last step length, behind an 88-byte
+ * header carrying a hash of the mesh (node coordinates, face nodes, face
+ * cells, face types) and FNV-1a 64 checksums of header and payload.  Load
+ * rejects (MST_EINVAL, state unchanged) files of another mesh, truncated
+ * or corrupted files.  Restarting from a checkpoint continues bit-for-bit
+ * like the uninterrupted run. */
+mst_status mst_checkpoint_save(mst_ctx *c, const char *path);
+mst_status mst_checkpoint_load(mst_ctx *c, const char *path);
+
+/* ------------------------------------------------------------------ */
 /* sparse LU-SGS / Gauss-Seidel sweeps (the reference's lusolver)      */
 /* ------------------------------------------------------------------ */
 typedef struct mst_lu mst_lu;

@@ -8,6 +8,8 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/capi.cu           the C ABI of include/mstcfd.h
   * csrc/noalloc.cu        the allocation-free solve entry point
   * csrc/lusgs.cu          level-scheduled LU-SGS / GS sweeps, --fmad=false
+  * csrc/io.cu             result writer (device node averaging) and
+                           checkpoint files, --fmad=false
 """
 import os
 import shutil
@@ -49,6 +51,7 @@ def _units():
         ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
         ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
         ("lusgs.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "lusgs.cu")]),
+        ("io.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "io.cu")]),
     ]
 
 

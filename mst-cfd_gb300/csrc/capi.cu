@@ -298,12 +298,8 @@ mst::StepArgs base_args(mst_ctx* c) {
   a.dt = c->p.dt;
   a.quirks = c->p.reference_quirks;
   a.limiter = c->p.limiter;
-  for (int k = 0; k < 4; ++k) a.inlet[k] = c->p.inlet_q[k];
-  a.viscous = c->p.viscous;
-  a.mu = c->p.mu;
-  a.lam = c->p.lambda;
-  a.kappa = c->p.kappa;
-  a.cv = c->p.cv;
+  mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa,
+                   c->p.cv);
   return a;
 }
 
@@ -698,6 +694,7 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
 mst_status mst_ctx_destroy(mst_ctx* c) {
   if (!c) return MST_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  mst_io_release(c);
   for (void* p : c->allocs) cudaFree(p);
   for (auto& p : c->pending) {
     cudaEventDestroy(p.a);

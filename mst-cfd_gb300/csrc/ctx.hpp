@@ -33,6 +33,9 @@ struct DevArrays {
       *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr;
 };
 
+struct mst_node_avg;  // result writer buffers (io.cu)
+void mst_io_release(struct mst_ctx* c);
+
 struct mst_ctx {
   const mst_mesh* mesh = nullptr;
   mst_params p{};
@@ -66,5 +69,6 @@ struct mst_ctx {
   bool timed = false;
   bool grad_valid = false;
   std::vector<void*> allocs;
+  mst_node_avg* node_avg = nullptr;
 };
 

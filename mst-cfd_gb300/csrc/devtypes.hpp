@@ -66,8 +66,30 @@ struct StepArgs {
   double inlet[4];
   int viscous;            // laminar viscous term on
   double mu, lam, kappa, cv;
+  // the same constants rounded to FP32 once on the host, so FP32 kernels
+  // convert nothing per face
+  float inlet_f[4];
+  float mu_f, lam_f, kappa_f, cv_f;
   double* partials;       // [n_tiles][kNormSlots] or nullptr
 };
+
+// Inflow state and viscous constants of a run into the step arguments.
+inline void set_physics(StepArgs& a, const double inlet[4], int viscous, double mu,
+                        double lam, double kappa, double cv) {
+  for (int k = 0; k < 4; ++k) {
+    a.inlet[k] = inlet[k];
+    a.inlet_f[k] = (float)inlet[k];
+  }
+  a.viscous = viscous;
+  a.mu = mu;
+  a.lam = lam;
+  a.kappa = kappa;
+  a.cv = cv;
+  a.mu_f = (float)mu;
+  a.lam_f = (float)lam;
+  a.kappa_f = (float)kappa;
+  a.cv_f = (float)cv;
+}
 
 // Precisions / schemes (mirrors of the public enums)
 enum { kPrecExact = 0, kPrecF64 = 1, kPrecF32 = 2 };

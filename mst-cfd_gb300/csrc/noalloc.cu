@@ -139,7 +139,8 @@ extern "C" mst_status mst_solve_device_noalloc(mst_ctx* c, const double* q_dev,
   a.stage = 0;
   a.quirks = c->p.reference_quirks;
   a.limiter = c->p.limiter;
-  for (int k = 0; k < 4; ++k) a.inlet[k] = c->p.inlet_q[k];
+  mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa,
+                   c->p.cv);
   a.partials = norms_dev ? partials : nullptr;
   e = exact ? mst::exact::launch_flux_update(c->p.precision, c->p.flux, c->p.order, c->dm, a,
                                              0, c->stream)

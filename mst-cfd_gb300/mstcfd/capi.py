@@ -121,6 +121,12 @@ def load():
         "mst_set_device": (C.c_int, [C.c_int]),
         "mst_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p]),
+        "mst_node_values": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "mst_write_plt": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+        "mst_write_cell_text": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "mst_read_cell_text": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "mst_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "mst_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p]),
         "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
                                     C.POINTER(C.c_void_p)]),
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),

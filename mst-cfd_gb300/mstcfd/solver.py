@@ -23,6 +23,7 @@ class Mesh:
         self.info = info
         self.n_cells, self.n_faces = info.n_cells, info.n_faces
         self.n_int_faces = info.n_int_faces
+        self.n_nodes = info.n_nodes
 
     @classmethod
     def read_msh(cls, path):
@@ -180,6 +181,34 @@ class Solver:
             capi.check(L.mst_profile_get(self._h, i, buf, 128, C.byref(n), C.byref(ms)))
             out[buf.value.decode()] = (n.value, ms.value)
         return out
+
+    # -- result writer and checkpoints (work/Work.cpp:204-319, :432-514) --
+    def node_values(self):
+        """Node averages of the current state: (node_q [nN][4], node_vars
+        [nN][6] = rho u v T p Ma), computed on the device."""
+        n = self.mesh.n_nodes
+        nq, nv = np.empty((n, 4)), np.empty((n, 6))
+        capi.check(capi.load().mst_node_values(self._h, capi.dptr(nq), capi.dptr(nv)))
+        return nq, nv
+
+    def write_plt(self, path, zone_t=0):
+        """Tecplot ASCII file of the current state (writedataRhoBasedMshNodePlt)."""
+        capi.check(capi.load().mst_write_plt(self._h, os.fsencode(path), int(zone_t)))
+
+    def write_cell_text(self, path):
+        """Text checkpoint, 4 numbers per cell (writedataCellContinue)."""
+        capi.check(capi.load().mst_write_cell_text(self._h, os.fsencode(path)))
+
+    def read_cell_text(self, path):
+        """State from a text checkpoint (readPbasedCellPlt)."""
+        capi.check(capi.load().mst_read_cell_text(self._h, os.fsencode(path)))
+
+    def checkpoint_save(self, path):
+        """Exact binary checkpoint of state and time."""
+        capi.check(capi.load().mst_checkpoint_save(self._h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        capi.check(capi.load().mst_checkpoint_load(self._h, os.fsencode(path)))
 
     def set_state_ptr(self, ptr, stride=4):
         """State in from a raw host pointer (e.g. a pinned buffer)."""

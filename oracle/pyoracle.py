@@ -89,6 +89,10 @@ def lib():
         L.om_lu_scalar.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp, _dp, _dp,
                                    _ip]
         L.om_lu_block.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp]
+        L.om_node_values.argtypes = [C.POINTER(_OMesh), _dp, C.c_int, C.c_double, _dp, _dp]
+        L.om_cell_nodes.argtypes = [C.POINTER(_OMesh), _ip, _ip]
+        L.om_write_plt.argtypes = [C.POINTER(_OMesh), _dp, C.c_double, C.c_int, C.c_char_p]
+        L.om_write_cell_text.argtypes = [C.c_int, _dp, C.c_char_p]
         _lib = L
     return _lib
 
@@ -315,3 +319,38 @@ def lu_block(dim, rows, cols, vals, b, x0):
     x = _f64(x0).copy()
     lib().om_lu_block(int(dim), len(rows), _i(rows), _i(cols), _d(vals), _d(b), _d(x))
     return x
+
+
+# ---------------------------------------------------------------------------
+# result writer and text checkpoint (Work.cpp:204-319, :483-514)
+# ---------------------------------------------------------------------------
+def node_values(mesh, q, quirks=1, cv=715.8):
+    """Node-averaged (node_q [nN][4], node_vars [nN][6] = rho u v T p Ma)."""
+    q = _f64(q)
+    nq = np.zeros((mesh.n_nodes, 4))
+    nv = np.zeros((mesh.n_nodes, 6))
+    rc = lib().om_node_values(mesh._p, _d(q), int(quirks), float(cv), _d(nq), _d(nv))
+    if rc != 0:
+        raise ValueError(f"oracle: node averaging refused (status {rc})")
+    return nq, nv
+
+
+def cell_nodes(mesh):
+    ptr = np.zeros(mesh.n_cells + 1, np.int32)
+    ids = np.zeros(4 * mesh.n_cells + 16, np.int32)
+    lib().om_cell_nodes(mesh._p, _i(ptr), _i(ids))
+    return ptr, ids[:ptr[-1]]
+
+
+def write_plt(mesh, q, path, zone_t=0, cv=715.8):
+    q = _f64(q)
+    rc = lib().om_write_plt(mesh._p, _d(q), float(cv), int(zone_t), os.fsencode(path))
+    if rc != 0:
+        raise ValueError(f"oracle: cannot write {path} (status {rc})")
+
+
+def write_cell_text(q, path):
+    q = _f64(q)
+    rc = lib().om_write_cell_text(len(q), _d(q), os.fsencode(path))
+    if rc != 0:
+        raise ValueError(f"oracle: cannot write {path} (status {rc})")

@@ -91,8 +91,18 @@ S="$OUT/ausm_o1/src"
 $CXX $CXXFLAGS -I"$S" "$S/lusolver/SparseSolverNUM.cpp" "$S/work/FUNCTION.cpp" \
   "$HERE/harness_lu.cpp" -o "$OUT/ref_lu"
 
+# Result writer and checkpoint files: Work.cpp's own members
+# (harness_io.cpp), linked with the first variant's objects.
+O="$OUT/ausm_o1/obj"
+$CXX $CXXFLAGS -I"$S" -c "$S/work/Work.cpp" -o "$O/work_Work.cpp.o"
+$CXX $CXXFLAGS -I"$S" -c "$HERE/harness_io.cpp" -o "$O/harness_io.o"
+objs=""
+for f in $SRCS; do objs="$objs $O/$(echo "$f" | tr '/' '_').o"; done
+$CXX $CXXFLAGS $objs "$O/work_Work.cpp.o" "$O/harness_io.o" -o "$OUT/ref_io"
+
 for v in ausm_o1 ausm_o2 roe_o1 roe_o2; do
   test -x "$OUT/ref_rho_$v"
 done
 test -x "$OUT/ref_lu"
+test -x "$OUT/ref_io"
 echo "build_ref: ok ($OUT)"

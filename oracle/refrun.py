@@ -112,3 +112,24 @@ def run_lu(mode, dim, rows, cols, ops, vals, b, x0):
     subprocess.run([os.path.join(_build.REF_OUT, "ref_lu"), inp, out],
                    check=True, stdout=subprocess.DEVNULL)
     return np.fromfile(out, dtype=np.float64)
+
+
+def run_io(mesh_path, q, zone_t=0, time_now=0):
+    """Run the reference's writer members (oracle/ref/harness_io.cpp) on
+    state q (file cell order).  Returns (plt bytes, cellPUVT bytes, the
+    state readPbasedCellPlt reads back)."""
+    if not _build.build_ref():
+        raise RuntimeError("reference sources not available")
+    d = tempfile.mkdtemp(prefix="mstio_")
+    qp = os.path.join(d, "q_in.f64")
+    np.ascontiguousarray(q, dtype=np.float64).tofile(qp)
+    subprocess.run([os.path.join(_build.REF_OUT, "ref_io"), os.path.abspath(mesh_path), d, qp,
+                    str(int(zone_t)), str(int(time_now))],
+                   check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    base = os.path.join(d, "result", f"mesh.msh_TIME4000_u0_t{int(time_now)}")
+    with open(base + ".plt", "rb") as f:
+        plt = f.read()
+    with open(base + ".cellPUVT", "rb") as f:
+        cell = f.read()
+    back = np.fromfile(os.path.join(d, "readback.bin"), dtype=np.float64).reshape(-1, 4)
+    return plt, cell, back

@@ -12,7 +12,9 @@ from its own sources into oracle/_ref (oracle/ref/build_ref.sh):
   * five steps of the reference's own time loop (Time::goNextTimeStep with
     its Sod initialisation and DT = 1/4000) and the L-infinity residual rows
     it logs.
-and lusolver.npz: sparse systems with a mesh's sparsity, inserted in a
+writer.npz: generated meshes with a random state, the Tecplot file and the
+text checkpoint the reference's own Work members write for them
+(oracle/ref/harness_io.cpp), and lusolver.npz: sparse systems with a mesh's sparsity, inserted in a
 shuffled order (setELE/addELE mixed, duplicates kept), solved by the
 reference's SparseSolverNUM::solveILUSGS / solveGS and
 SparseSolver<Matrix4d, Vector4d>::solveILU (oracle/ref/harness_lu.cpp).
@@ -128,9 +130,36 @@ def make_lu():
     return path
 
 
+def io_cases():
+    yield "tri_iow", mg.reorient(mg.tri_box(16, 9, 1.0, 0.6, jitter=0.2, seed=3, left=mg.INLET,
+                                           right=mg.OUTLET, bottom=mg.WALL, top=mg.WALL),
+                                "random", seed=4)
+    yield "quad_strip", mg.reorient(mg.sod_strip(24, 3, ends=mg.OUTLET), "fluent")
+
+
+def make_io():
+    out = {}
+    for name, mesh in io_cases():
+        d = tempfile.mkdtemp(prefix="golden_io_")
+        msh = os.path.join(d, name + ".msh")
+        mg.write_msh(msh, mesh, crlf=True)
+        q = mg.random_state(int(mesh["n_cells"]), seed=21)
+        plt, cell, back = refrun.run_io(msh, q, zone_t=7, time_now=5)
+        out[name + "_msh"] = np.frombuffer(open(msh, "rb").read(), np.uint8)
+        out[name + "_q"] = q
+        out[name + "_plt"] = np.frombuffer(plt, np.uint8)
+        out[name + "_cell"] = np.frombuffer(cell, np.uint8)
+        out[name + "_readback"] = back
+    path = os.path.join(OUT, "writer.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 if __name__ == "__main__":
     for name, mesh in cases():
         p = make(name, mesh)
         print(p, os.path.getsize(p))
     p = make_lu()
+    print(p, os.path.getsize(p))
+    p = make_io()
     print(p, os.path.getsize(p))
