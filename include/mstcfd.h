@@ -234,6 +234,76 @@ mst_status mst_get_time(mst_ctx *c, double *t);
 mst_status mst_last_timing(mst_ctx *c, double *ms, int *launches);
 
 /* ------------------------------------------------------------------ */
+/* batched steady solves (implicit LU-SGS)                             */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference, whose density-based path is explicit
+ * only: many independent cases, each a mesh with its own inflow state and
+ * transport coefficients, iterated together on one GPU to a residual
+ * tolerance by matrix-free LU-SGS (Yoon-Jameson: scalar diagonal from the
+ * spectral radii, Euler-flux differences off the diagonal), with local
+ * steps from a per-case CFL number that grows as the residual falls
+ * (switched evolution relaxation), and Gauss-Seidel sweeps over colour
+ * groups of the cell adjacency (one launch per colour and direction).
+ * The residual is the corrected-mode (reference_quirks = 0) residual of
+ * mst_params, in its precision; the sweeps and the state are FP64. */
+typedef struct mst_batch mst_batch;
+
+typedef struct mst_case_params {
+  double inlet_q[4];               /* type-10 boundary state of the case */
+  double mu, lambda, kappa, cv;    /* transport coefficients (viscous runs) */
+} mst_case_params;
+
+typedef struct mst_implicit_params {
+  double cfl0;      /* CFL of the first iteration */
+  double cfl_max;   /* ceiling of CFL = cfl0 * L2_first / L2 */
+  double omega;     /* LU-SGS relaxation of the spectral radii (>= 1) */
+  double tol;       /* a case has converged when L2 <= tol * L2_first */
+  int max_iter;     /* iteration limit of mst_batch_solve */
+  int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
+  int autotune;     /* time the sweep block sizes once and keep the fastest */
+  int reserved[5];
+} mst_implicit_params;
+
+/* cfl0 5, cfl_max 200, omega 1.5, tol 1e-8, max_iter 20000,
+ * graph_iters 20, autotune on. */
+void mst_implicit_params_default(mst_implicit_params *p);
+
+typedef struct mst_batch_info_t {
+  int n_cases, n_cells, n_faces, n_colors, sweep_threads, graph_iters;
+} mst_batch_info_t;
+
+typedef struct mst_batch_result {
+  int iterations;        /* iterations run by this call */
+  int total_iterations;  /* since the state was set */
+  int n_converged;       /* cases at tolerance */
+  double ms;             /* device time of the call */
+} mst_batch_result;
+
+/* Joins the meshes into one device mesh (cases keep their cells together)
+ * and allocates the batch.  L2 = sqrt(mean over the case's cells of
+ * (R_rho / V)^2), normalised by its value at the first iteration. */
+mst_status mst_batch_create(const mst_mesh *const *meshes,
+                            const mst_case_params *cases, int n_cases,
+                            const mst_params *p, const mst_implicit_params *ip,
+                            mst_batch **out);
+mst_status mst_batch_destroy(mst_batch *b);
+mst_status mst_batch_info(const mst_batch *b, mst_batch_info_t *info);
+/* Colour of every cell, cases in order, file numbering within a case. */
+mst_status mst_batch_colors(const mst_batch *b, int *color);
+/* States of all cases, cases in order, rows of 4 doubles; setting the
+ * state restarts the convergence bookkeeping. */
+mst_status mst_batch_set_state(mst_batch *b, const double *q);
+mst_status mst_batch_get_state(mst_batch *b, double *q);
+/* Exactly n iterations (no convergence stop, no graph). */
+mst_status mst_batch_iterate(mst_batch *b, int n);
+/* Iterates until every case has converged or max_iter iterations ran. */
+mst_status mst_batch_solve(mst_batch *b, mst_batch_result *res);
+/* Per case: the iteration at which it converged (-1: not yet), the first
+ * and the latest L2 (each nullable). */
+mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
+                                 double *first_l2, double *last_l2);
+
+/* ------------------------------------------------------------------ */
 /* result writer and checkpoint files                                  */
 /* ------------------------------------------------------------------ */
 /* Node averages of the current state, computed on the device as

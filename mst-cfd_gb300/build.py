@@ -10,6 +10,8 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/lusgs.cu          level-scheduled LU-SGS / GS sweeps, --fmad=false
   * csrc/io.cu             result writer (device node averaging) and
                            checkpoint files, --fmad=false
+  * csrc/batch.cu          batched steady solves (LU-SGS orchestration,
+                           CUDA graph, sweep autotuning)
 """
 import os
 import shutil
@@ -52,6 +54,7 @@ def _units():
         ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
         ("lusgs.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "lusgs.cu")]),
         ("io.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "io.cu")]),
+        ("batch.o", [nv] + common + ["-c", os.path.join(CSRC, "batch.cu")]),
     ]
 
 

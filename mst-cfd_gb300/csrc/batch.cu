@@ -1,0 +1,532 @@
+// Batched steady solves: many independent cases (meshes with their own
+// inflow state and transport coefficients) iterated together to a
+// residual tolerance by matrix-free LU-SGS (implicit.inc).
+//
+// The cases are joined into one disjoint-union mesh (mst::build_union):
+// each case keeps its own Morton ordering and occupies a contiguous range
+// of device cells, every face carries its case id, so the residual kernels
+// of the explicit path run unchanged over all cases at once and take the
+// inflow state and viscosity of each face's case from a table.  Per
+// iteration: gradient, residual, per-case norms and CFL (one block per
+// case), then the forward and backward LU-SGS sweeps, one launch per
+// colour of the cell adjacency.  graph_iters iterations are captured once
+// into a CUDA graph and replayed until every case has converged.  The
+// sweep block size is chosen at creation by timing the candidates (the
+// sweeps give the same result for any block size).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace {
+
+#define B_CU(call)                                                             \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return mst_internal_fail(MST_ECUDA, std::string(#call) + ": " +          \
+                                              cudaGetErrorString(e_));         \
+  } while (0)
+
+__global__ void k_batch_gather(const double4_32a* __restrict__ src,
+                               const int* __restrict__ idx, double4_32a* __restrict__ dst,
+                               int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[idx[i]];
+}
+__global__ void k_batch_reset(int n_cases, double cfl0, double* cfl, int* conv_iter,
+                              int* n_conv, int* iter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_cases) {
+    cfl[i] = cfl0;
+    conv_iter[i] = -1;
+  }
+  if (i == 0) {
+    *n_conv = 0;
+    *iter = 0;
+  }
+}
+
+}  // namespace
+
+struct mst_batch {
+  mst_mesh* mesh = nullptr;  // the union mesh (owned)
+  mst_ctx* ctx = nullptr;    // context on it (owned)
+  int n_cases = 0;
+  int n_colors = 0;
+  int threads = 128;
+  mst_implicit_params ip{};
+  std::vector<int> color_off;    // [n_colors + 1] into color_cells
+  std::vector<int> color_file;   // colour of every union cell, file order
+  int* color = nullptr;          // device order
+  int* color_cells = nullptr;
+  int* c_case = nullptr;
+  int* case_first = nullptr;
+  double* case_tab = nullptr;
+  float* case_tab_f = nullptr;
+  double *cfl = nullptr, *first = nullptr, *last = nullptr;
+  int *conv_iter = nullptr, *n_conv = nullptr, *iter = nullptr;
+  double4_32a* dq = nullptr;
+  double* diag = nullptr;
+  int cur = 0;                   // which of ctx->q_old / q_new holds Q
+  cudaGraphExec_t graph = nullptr;
+  int graph_iters = 0;
+  int graph_cur = 0;             // the buffer the captured iterations start from
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+template <class T>
+mst_status balloc(mst_batch* b, T** p, size_t bytes) {
+  B_CU(cudaMalloc((void**)p, std::max<size_t>(bytes, 256)));
+  b->allocs.push_back(*p);
+  return MST_OK;
+}
+
+template <class T>
+mst_status bupload(mst_batch* b, T** p, const std::vector<T>& v) {
+  mst_status s = balloc(b, p, v.size() * sizeof(T));
+  if (s) return s;
+  if (!v.empty()) B_CU(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return MST_OK;
+}
+
+double4_32a* qbuf(mst_batch* b, int which) { return which ? b->ctx->q_new : b->ctx->q_old; }
+float4* qfbuf(mst_batch* b, int which) {
+  if (b->ctx->p.precision != MST_PREC_FP32) return nullptr;
+  return which ? b->ctx->qf_new : b->ctx->qf_old;
+}
+
+bool exact(const mst_batch* b) { return b->ctx->p.precision == MST_PREC_FP64_EXACT; }
+
+// the residual R(Q) of the current state into ctx->r
+mst_status enqueue_residual(mst_batch* b, int which) {
+  mst_ctx* c = b->ctx;
+  const int prec = c->p.precision;
+  cudaStream_t s = c->stream;
+  const double4_32a* q = qbuf(b, which);
+  const float4* qf = qfbuf(b, which);
+  cudaError_t e = cudaSuccess;
+  if (c->p.order == 2) {
+    if (exact(b)) e = mst::exact::launch_gradient(prec, c->dm, q, c->grad, 0, s);
+    else if (qf)
+      e = mst::fast::launch_gradient_dt(prec, c->dm, q, qf, c->grad, 0, 0.0, nullptr, nullptr,
+                                        nullptr, s);
+    else e = mst::fast::launch_gradient(prec, c->dm, q, c->grad, 0, s);
+    if (e != cudaSuccess)
+      return mst_internal_fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
+  }
+  mst::StepArgs a{};
+  a.q = q;
+  a.qf = qf;
+  a.grad = c->grad;
+  a.r_out = c->r;
+  a.quirks = 0;
+  a.limiter = c->p.limiter;
+  mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa, c->p.cv);
+  a.case_tab = b->case_tab;
+  a.case_tab_f = b->case_tab_f;
+  e = exact(b) ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
+               : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
+  if (e != cudaSuccess)
+    return mst_internal_fail(MST_ECUDA, std::string("residual: ") + cudaGetErrorString(e));
+  return MST_OK;
+}
+
+mst::LusgsArgs sweep_args(mst_batch* b, int which) {
+  mst_ctx* c = b->ctx;
+  mst::LusgsArgs la{};
+  la.q = qbuf(b, which);
+  la.r = c->r;
+  la.dq = b->dq;
+  la.diag = b->diag;
+  la.qn = qbuf(b, 1 - which);
+  la.qfn = qfbuf(b, 1 - which);
+  la.color = b->color;
+  la.c_case = b->c_case;
+  la.cfl = b->cfl;
+  la.case_tab = b->case_tab;
+  la.mu = c->p.mu;
+  la.viscous = c->p.viscous;
+  la.omega = b->ip.omega;
+  return la;
+}
+
+mst_status enqueue_sweeps(mst_batch* b, int which, int threads) {
+  mst_ctx* c = b->ctx;
+  mst::LusgsArgs la = sweep_args(b, which);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = 0; i < b->n_colors; ++i) {
+      const int col = pass == 0 ? i : b->n_colors - 1 - i;
+      la.col = col;
+      la.cells = b->color_cells + b->color_off[col];
+      la.n = b->color_off[col + 1] - b->color_off[col];
+      cudaError_t e;
+      if (pass == 0)
+        e = exact(b) ? mst::exact::lusgs_forward_t(c->dm, la, threads, c->stream)
+                     : mst::fast::lusgs_forward_t(c->dm, la, threads, c->stream);
+      else
+        e = exact(b) ? mst::exact::lusgs_backward_t(c->dm, la, threads, c->stream)
+                     : mst::fast::lusgs_backward_t(c->dm, la, threads, c->stream);
+      if (e != cudaSuccess)
+        return mst_internal_fail(MST_ECUDA, std::string("lusgs sweep: ") + cudaGetErrorString(e));
+    }
+  }
+  return MST_OK;
+}
+
+// one implicit iteration from buffer `which` into the other one
+mst_status enqueue_iteration(mst_batch* b, int which) {
+  mst_status st = enqueue_residual(b, which);
+  if (st) return st;
+  mst::CaseNormArgs na{};
+  na.r = b->ctx->r;
+  na.case_first = b->case_first;
+  na.first = b->first;
+  na.last = b->last;
+  na.cfl = b->cfl;
+  na.conv_iter = b->conv_iter;
+  na.n_conv = b->n_conv;
+  na.iter = b->iter;
+  na.cfl0 = b->ip.cfl0;
+  na.cfl_max = b->ip.cfl_max;
+  na.tol = b->ip.tol;
+  cudaError_t e = exact(b) ? mst::exact::case_norms_t(b->ctx->dm, na, b->n_cases, b->ctx->stream)
+                           : mst::fast::case_norms_t(b->ctx->dm, na, b->n_cases, b->ctx->stream);
+  if (e != cudaSuccess)
+    return mst_internal_fail(MST_ECUDA, std::string("case norms: ") + cudaGetErrorString(e));
+  return enqueue_sweeps(b, which, b->threads);
+}
+
+// Times the sweeps of the current state for each candidate block size and
+// keeps the fastest.  Only the scratch buffers (dq, diag, the other state
+// buffer) are written, so the state and the iteration count are untouched.
+mst_status autotune(mst_batch* b) {
+  mst_ctx* c = b->ctx;
+  mst_status st = enqueue_residual(b, b->cur);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  B_CU(cudaEventCreate(&e0));
+  B_CU(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int pick = 128;
+  for (int th : {64, 128, 256}) {
+    for (int rep = 0; rep < 2; ++rep) {  // the first repetition warms up
+      B_CU(cudaEventRecord(e0, c->stream));
+      st = enqueue_sweeps(b, b->cur, th);
+      if (st) break;
+      B_CU(cudaEventRecord(e1, c->stream));
+      B_CU(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      B_CU(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep == 1 && ms < best) {
+        best = ms;
+        pick = th;
+      }
+    }
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  b->threads = pick;
+  return MST_OK;
+}
+
+mst_status build_graph(mst_batch* b, int k) {
+  mst_ctx* c = b->ctx;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  B_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  mst_status st = MST_OK;
+  int which = b->cur;
+  for (int i = 0; i < k && !st; ++i) {
+    st = enqueue_iteration(b, which);
+    which = 1 - which;
+  }
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess)
+    return mst_internal_fail(MST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return mst_internal_fail(MST_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  b->graph_iters = k;
+  b->graph_cur = b->cur;
+  return MST_OK;
+}
+
+mst_status reset_progress(mst_batch* b) {
+  k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, b->ctx->stream>>>(
+      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->n_conv, b->iter);
+  B_CU(cudaGetLastError());
+  return MST_OK;
+}
+
+mst_status run_iterations(mst_batch* b, int n) {
+  for (int i = 0; i < n; ++i) {
+    mst_status st = enqueue_iteration(b, b->cur);
+    if (st) return st;
+    b->cur = 1 - b->cur;
+  }
+  return MST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mst_implicit_params_default(mst_implicit_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->cfl0 = 5.0;
+  p->cfl_max = 200.0;
+  p->omega = 1.5;
+  p->tol = 1e-8;
+  p->max_iter = 20000;
+  p->graph_iters = 20;
+  p->autotune = 1;
+}
+
+mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params* cases,
+                            int n_cases, const mst_params* p, const mst_implicit_params* ip,
+                            mst_batch** out) {
+  if (!meshes || !cases || !p || !ip || !out || n_cases <= 0)
+    return mst_internal_fail(MST_EINVAL, "NULL argument or no cases");
+  *out = nullptr;
+  if (p->reference_quirks)
+    return mst_internal_fail(MST_EINVAL, "batches run the corrected scheme (reference_quirks = 0)");
+  if (!(ip->cfl0 > 0) || !(ip->cfl_max >= ip->cfl0) || !(ip->omega >= 1.0) || !(ip->tol > 0) ||
+      ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1))
+    return mst_internal_fail(MST_EINVAL,
+                             "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
+                             "tol > 0, max_iter >= 0, graph_iters >= 0 and even");
+  std::unique_ptr<mst_batch> b(new mst_batch());
+  b->ip = *ip;
+  b->n_cases = n_cases;
+  std::vector<const mst::HostMesh*> parts;
+  for (int k = 0; k < n_cases; ++k) {
+    if (!meshes[k]) return mst_internal_fail(MST_EINVAL, "NULL mesh in the batch");
+    parts.push_back(&meshes[k]->host);
+  }
+  b->mesh = new mst_mesh();
+  std::string err;
+  int rc = mst::build_union(parts, &b->mesh->host, &err);
+  if (rc == mst::kOk) rc = mst::build_layout(b->mesh->host, true, &b->mesh->lay, &err);
+  if (rc != mst::kOk) {
+    delete b->mesh;
+    b->mesh = nullptr;
+    return mst_internal_fail(rc == mst::kEMesh ? MST_EMESH : MST_EINVAL, err);
+  }
+  mst_status st = mst_ctx_create(b->mesh, p, &b->ctx);
+  auto cleanup = [&]() {
+    if (b->ctx) mst_ctx_destroy(b->ctx);
+    for (void* q : b->allocs) cudaFree(q);
+    delete b->mesh;
+  };
+  if (st) {
+    cleanup();
+    return st;
+  }
+  const mst::HostMesh& h = b->mesh->host;
+  const mst::DevLayout& L = b->mesh->lay;
+  const int nC = h.n_cells;
+  // greedy colouring in file order (the oracle's om_greedy_colors)
+  b->color_file.assign(nC, -1);
+  int ncol = 0;
+  for (int c = 0; c < nC; ++c) {
+    unsigned used = 0;
+    for (int k = h.cell_ptr[c]; k < h.cell_ptr[c + 1]; ++k) {
+      const int f = h.cell_faces[k];
+      if (h.face_cells[2 * f + 1] < 0) continue;
+      const int nb = h.cell_nb[k];
+      if (nb != c && b->color_file[nb] >= 0 && b->color_file[nb] < 32)
+        used |= 1u << b->color_file[nb];
+    }
+    int pick = 0;
+    while (used & (1u << pick)) ++pick;
+    b->color_file[c] = pick;
+    ncol = std::max(ncol, pick + 1);
+  }
+  b->n_colors = ncol;
+  std::vector<int> color_dev(nC), c_case(nC), case_first(n_cases + 1);
+  for (int c = 0; c < nC; ++c) color_dev[L.cell_perm[c]] = b->color_file[c];
+  for (int k = 0; k < n_cases; ++k)
+    for (int c = h.case_cells[k]; c < h.case_cells[k + 1]; ++c) c_case[L.cell_perm[c]] = k;
+  // device cells of case k are contiguous (per-case Morton ranges)
+  for (int k = 0; k <= n_cases; ++k) case_first[k] = h.case_cells[k];
+  b->color_off.assign(ncol + 1, 0);
+  for (int d = 0; d < nC; ++d) b->color_off[color_dev[d] + 1]++;
+  for (int i = 0; i < ncol; ++i) b->color_off[i + 1] += b->color_off[i];
+  std::vector<int> fill(b->color_off.begin(), b->color_off.end() - 1), cells(nC);
+  for (int d = 0; d < nC; ++d) cells[fill[color_dev[d]]++] = d;
+  std::vector<double> tab((size_t)mst::kCaseWords * n_cases);
+  std::vector<float> tabf(tab.size());
+  for (int k = 0; k < n_cases; ++k) {
+    const mst_case_params& cp = cases[k];
+    const double v[8] = {cp.inlet_q[0], cp.inlet_q[1], cp.inlet_q[2], cp.inlet_q[3],
+                         cp.mu, cp.lambda, cp.kappa, cp.cv};
+    for (int j = 0; j < 8; ++j) {
+      tab[8 * (size_t)k + j] = v[j];
+      tabf[8 * (size_t)k + j] = (float)v[j];
+    }
+  }
+  if ((st = bupload(b.get(), &b->color, color_dev)) ||
+      (st = bupload(b.get(), &b->color_cells, cells)) ||
+      (st = bupload(b.get(), &b->c_case, c_case)) ||
+      (st = bupload(b.get(), &b->case_first, case_first)) ||
+      (st = bupload(b.get(), &b->case_tab, tab)) ||
+      (st = bupload(b.get(), &b->case_tab_f, tabf)) ||
+      (st = balloc(b.get(), &b->cfl, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->first, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->last, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->conv_iter, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->n_conv, sizeof(int))) ||
+      (st = balloc(b.get(), &b->iter, sizeof(int))) ||
+      (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
+      (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
+      (st = reset_progress(b.get()))) {
+    cleanup();
+    return st;
+  }
+  if (cudaStreamSynchronize(b->ctx->stream) != cudaSuccess) {
+    cleanup();
+    return mst_internal_fail(MST_ECUDA, "batch setup failed");
+  }
+  *out = b.release();
+  return MST_OK;
+}
+
+mst_status mst_batch_destroy(mst_batch* b) {
+  if (!b) return MST_OK;
+  if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->ctx) mst_ctx_destroy(b->ctx);
+  delete b->mesh;
+  delete b;
+  return MST_OK;
+}
+
+mst_status mst_batch_info(const mst_batch* b, mst_batch_info_t* info) {
+  if (!b || !info) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  info->n_cases = b->n_cases;
+  info->n_cells = b->mesh->host.n_cells;
+  info->n_faces = b->mesh->host.n_faces;
+  info->n_colors = b->n_colors;
+  info->sweep_threads = b->threads;
+  info->graph_iters = b->graph_iters;
+  return MST_OK;
+}
+
+mst_status mst_batch_colors(const mst_batch* b, int* color) {
+  if (!b || !color) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  std::memcpy(color, b->color_file.data(), sizeof(int) * b->color_file.size());
+  return MST_OK;
+}
+
+mst_status mst_batch_set_state(mst_batch* b, const double* q) {
+  if (!b || !q) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  mst_status st = mst_set_state(b->ctx, q, 4);
+  if (st) return st;
+  b->cur = 0;
+  st = reset_progress(b);
+  if (st) return st;
+  B_CU(cudaStreamSynchronize(b->ctx->stream));
+  return MST_OK;
+}
+
+mst_status mst_batch_get_state(mst_batch* b, double* q) {
+  if (!b || !q) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  mst_ctx* c = b->ctx;
+  const int nC = c->dm.n_cells;
+  k_batch_gather<<<(nC + 255) / 256, 256, 0, c->stream>>>(qbuf(b, b->cur), c->d.cell_perm,
+                                                           c->stage_in, nC);
+  B_CU(cudaGetLastError());
+  B_CU(cudaMemcpyAsync(q, c->stage_in, sizeof(double4_32a) * (size_t)nC, cudaMemcpyDeviceToHost,
+                       c->stream));
+  B_CU(cudaStreamSynchronize(c->stream));
+  return MST_OK;
+}
+
+mst_status mst_batch_iterate(mst_batch* b, int n) {
+  if (!b || n < 0) return mst_internal_fail(MST_EINVAL, "bad argument");
+  mst_status st = run_iterations(b, n);
+  if (st) return st;
+  B_CU(cudaStreamSynchronize(b->ctx->stream));
+  return MST_OK;
+}
+
+mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
+  if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
+  mst_ctx* c = b->ctx;
+  mst_status st;
+  if (b->ip.autotune && b->graph_iters == 0) {
+    st = autotune(b);
+    if (st) return st;
+  }
+  const int k = b->ip.graph_iters;
+  if (k > 0 && (b->graph_iters != k || b->graph_cur != b->cur)) {
+    // the kernels' one-time attribute setup runs before capture
+    st = enqueue_residual(b, b->cur);
+    if (st) return st;
+    B_CU(cudaStreamSynchronize(c->stream));
+    st = build_graph(b, k);
+    if (st) return st;
+  }
+  int h[2] = {0, 0};
+  B_CU(cudaMemcpy(&h[0], b->iter, sizeof(int), cudaMemcpyDeviceToHost));
+  const int start = h[0];
+  B_CU(cudaEventRecord(c->ev0, c->stream));
+  int done = 0, iters = 0;
+  while (iters < b->ip.max_iter) {
+    if (k > 0 && iters + k <= b->ip.max_iter) {
+      B_CU(cudaGraphLaunch(b->graph, c->stream));
+      iters += k;  // k is even: the state is back in the same buffer
+    } else {
+      st = run_iterations(b, 1);
+      if (st) return st;
+      iters += 1;
+    }
+    B_CU(cudaMemcpyAsync(&h[1], b->n_conv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    B_CU(cudaStreamSynchronize(c->stream));
+    done = h[1];
+    if (done >= b->n_cases) break;
+  }
+  B_CU(cudaEventRecord(c->ev1, c->stream));
+  B_CU(cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  B_CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (res) {
+    res->iterations = iters;
+    res->total_iterations = start + iters;
+    res->n_converged = done;
+    res->ms = ms;
+  }
+  return MST_OK;
+}
+
+mst_status mst_batch_case_status(mst_batch* b, int* conv_iter, double* first_l2,
+                                 double* last_l2) {
+  if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
+  const size_t n = (size_t)b->n_cases;
+  if (conv_iter) B_CU(cudaMemcpy(conv_iter, b->conv_iter, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (first_l2) B_CU(cudaMemcpy(first_l2, b->first, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (last_l2) B_CU(cudaMemcpy(last_l2, b->last, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return MST_OK;
+}
+
+}  // extern "C"

@@ -70,8 +70,14 @@ struct StepArgs {
   // convert nothing per face
   float inlet_f[4];
   float mu_f, lam_f, kappa_f, cv_f;
+  // batches: per case kCaseWords numbers (inflow state[4], mu, lambda,
+  // kappa, cv), indexed by the case id in the face's info word; nullptr
+  // for a single case (the scalars above)
+  const double* case_tab;
+  const float* case_tab_f;
   double* partials;       // [n_tiles][kNormSlots] or nullptr
 };
+constexpr int kCaseWords = 8;
 
 // Inflow state and viscous constants of a run into the step arguments.
 inline void set_physics(StepArgs& a, const double inlet[4], int viscous, double mu,
@@ -90,6 +96,44 @@ inline void set_physics(StepArgs& a, const double inlet[4], int viscous, double 
   a.kappa_f = (float)kappa;
   a.cv_f = (float)cv;
 }
+
+// Arguments of one LU-SGS sweep launch (implicit.inc).
+struct LusgsArgs {
+  const double4_32a* q;    // Q^n, device order
+  const double4_32a* r;    // R(Q^n)
+  double4_32a* dq;         // dQ* after the forward sweep, dQ after the backward
+  double* diag;            // D_i (written by the forward sweep)
+  double4_32a* qn;         // Q^{n+1} (backward sweep)
+  float4* qfn;             // its FP32 copy, or nullptr
+  const int* color;        // colour of every device cell
+  const int* cells;        // the cells of the colour being swept
+  int n;                   // their number
+  int col;                 // the colour
+  const int* c_case;       // case of every device cell (nullptr: case 0)
+  const double* cfl;       // CFL number of every case
+  const double* case_tab;  // per-case coefficients (mu at [4]) or nullptr
+  double mu;               // viscosity of a single case
+  int viscous;
+  double omega;
+};
+
+// Per-case residual norms and the CFL of the next iteration, one block per
+// case over its contiguous device cells: L2 = sqrt(mean (R_rho / V)^2)
+// (fixed-order block reduction: deterministic).  The first iteration's L2
+// is kept; CFL = clamp(cfl0 * L2_first / L2, cfl0, cfl_max) (switched
+// evolution relaxation); a case converges at the first iteration whose
+// L2 / L2_first < tol.
+struct CaseNormArgs {
+  const double4_32a* r;
+  const int* case_first;   // [n_cases + 1] device cell ranges
+  double* first;           // [n_cases] L2 of iteration 0
+  double* last;            // [n_cases] latest L2
+  double* cfl;             // [n_cases]
+  int* conv_iter;          // [n_cases] -1 until converged
+  int* n_conv;             // number of converged cases
+  int* iter;               // iteration counter (advanced by k_iter_advance)
+  double cfl0, cfl_max, tol;
+};
 
 // Precisions / schemes (mirrors of the public enums)
 enum { kPrecExact = 0, kPrecF64 = 1, kPrecF32 = 2 };
@@ -118,6 +162,12 @@ enum { kFluxAusm = 0, kFluxRoe = 1 };
                                  const double4_32a* q, double cfl,            \
                                  double* dt_cell, double* partials,           \
                                  cudaStream_t s);                             \
+  cudaError_t lusgs_forward_t(const DevMesh& m, const LusgsArgs& a,          \
+                              int threads, cudaStream_t s);                   \
+  cudaError_t lusgs_backward_t(const DevMesh& m, const LusgsArgs& a,         \
+                               int threads, cudaStream_t s);                  \
+  cudaError_t case_norms_t(const DevMesh& m, const CaseNormArgs& a,          \
+                           int n_cases, cudaStream_t s);                      \
   }
 
 MST_DECLARE_LAUNCHERS(exact)

@@ -8,6 +8,7 @@ namespace mst {
 namespace exact {
 constexpr bool kExactArith = true;
 #include "kernels.inc"
+#include "implicit.inc"
 
 cudaError_t launch_gradient(int, const DevMesh& m, const double4_32a* q,
                             void* grad, int quirks, cudaStream_t s) {

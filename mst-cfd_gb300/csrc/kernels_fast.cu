@@ -8,6 +8,7 @@ namespace mst {
 namespace fast {
 constexpr bool kExactArith = false;
 #include "kernels.inc"
+#include "implicit.inc"
 
 cudaError_t launch_gradient(int prec, const DevMesh& m, const double4_32a* q,
                             void* grad, int quirks, cudaStream_t s) {

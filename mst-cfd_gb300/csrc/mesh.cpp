@@ -441,22 +441,28 @@ int build_layout(const HostMesh& m, bool renumber, DevLayout* L,
   L->cell_iperm.resize(nC);
   std::iota(L->cell_iperm.begin(), L->cell_iperm.end(), 0);
   if (renumber && nC > kTileCells) {
-    double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
-    for (int c = 0; c < nC; ++c)
-      for (int d = 0; d < 2; ++d) {
-        lo[d] = std::min(lo[d], m.cell_ctr[2 * c + d]);
-        hi[d] = std::max(hi[d], m.cell_ctr[2 * c + d]);
-      }
+    // one Morton curve per case (a single mesh is one case); cases keep
+    // their order, so the device cells of a case are contiguous
+    std::vector<int> seg = m.case_cells;
+    if (seg.empty()) seg = {0, nC};
     std::vector<uint64_t> key(nC);
-    for (int c = 0; c < nC; ++c) {
-      uint32_t q[2];
-      for (int d = 0; d < 2; ++d) {
-        double span = hi[d] - lo[d];
-        double u = span > 0 ? (m.cell_ctr[2 * c + d] - lo[d]) / span : 0.0;
-        if (!(u >= 0)) u = 0;  // NaN centroids go first
-        q[d] = (uint32_t)std::min(65535.0, std::floor(u * 65536.0));
+    for (size_t s = 0; s + 1 < seg.size(); ++s) {
+      double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
+      for (int c = seg[s]; c < seg[s + 1]; ++c)
+        for (int d = 0; d < 2; ++d) {
+          lo[d] = std::min(lo[d], m.cell_ctr[2 * c + d]);
+          hi[d] = std::max(hi[d], m.cell_ctr[2 * c + d]);
+        }
+      for (int c = seg[s]; c < seg[s + 1]; ++c) {
+        uint32_t q[2];
+        for (int d = 0; d < 2; ++d) {
+          double span = hi[d] - lo[d];
+          double u = span > 0 ? (m.cell_ctr[2 * c + d] - lo[d]) / span : 0.0;
+          if (!(u >= 0)) u = 0;  // NaN centroids go first
+          q[d] = (uint32_t)std::min(65535.0, std::floor(u * 65536.0));
+        }
+        key[c] = ((uint64_t)s << 32) | spread_bits(q[0]) | (spread_bits(q[1]) << 1);
       }
-      key[c] = spread_bits(q[0]) | (spread_bits(q[1]) << 1);
     }
     std::stable_sort(L->cell_iperm.begin(), L->cell_iperm.end(),
                      [&](int a, int b) { return key[a] < key[b]; });
@@ -515,6 +521,7 @@ int build_layout(const HostMesh& m, bool renumber, DevLayout* L,
     L->f_c0c1[2 * df] = L->cell_perm[c0];
     L->f_c0c1[2 * df + 1] = c1 >= 0 ? L->cell_perm[c1] : -1;
     int info = face_kind(m.face_type[f]);
+    if (!m.face_case.empty()) info |= m.face_case[f] << kInfoCaseShift;
     for (int d = 0; d < 2; ++d) {
       if (m.face_flag[2 * f + d]) info |= 1 << (kInfoFlagRef + d);
       if (m.face_flag_geo[2 * f + d]) info |= 1 << (kInfoFlagGeo + d);
@@ -590,6 +597,78 @@ int build_layout(const HostMesh& m, bool renumber, DevLayout* L,
       }
     }
   }
+  return kOk;
+}
+
+int build_union(const std::vector<const HostMesh*>& parts, HostMesh* out,
+                std::string* err) {
+  HostMesh& u = *out;
+  u = HostMesh{};
+  if (parts.empty()) {
+    *err = "empty batch";
+    return kEInval;
+  }
+  const bool per = std::any_of(parts.begin(), parts.end(),
+                               [](const HostMesh* p) { return p->periodic(); });
+  u.case_cells.push_back(0);
+  int zid = 1;
+  for (size_t k = 0; k < parts.size(); ++k) {
+    const HostMesh& p = *parts[k];
+    if (!p.face_case.empty()) {
+      *err = "a batch part is itself a batch";
+      return kEInval;
+    }
+    const int on = u.n_nodes, oc = u.n_cells, of = u.n_faces;
+    const int ot = (int)u.cell_faces.size();
+    u.node_xy.insert(u.node_xy.end(), p.node_xy.begin(), p.node_xy.end());
+    for (int v : p.face_nodes) u.face_nodes.push_back(v + on);
+    for (size_t i = 0; i < p.face_cells.size(); ++i) {
+      const int v = p.face_cells[i];
+      u.face_cells.push_back(v >= 0 ? v + oc : -1);
+    }
+    u.face_type.insert(u.face_type.end(), p.face_type.begin(), p.face_type.end());
+    if (per) {
+      if (p.periodic()) u.c1_shift.insert(u.c1_shift.end(), p.c1_shift.begin(), p.c1_shift.end());
+      else u.c1_shift.insert(u.c1_shift.end(), 2 * (size_t)p.n_faces, 0.0);
+    }
+    auto cat = [](auto& dst, const auto& src) { dst.insert(dst.end(), src.begin(), src.end()); };
+    cat(u.face_ctr, p.face_ctr);
+    cat(u.face_dir, p.face_dir);
+    cat(u.face_area, p.face_area);
+    cat(u.face_eta0, p.face_eta0);
+    cat(u.face_dac, p.face_dac);
+    cat(u.face_flag, p.face_flag);
+    cat(u.face_flag_geo, p.face_flag_geo);
+    if (u.cell_ptr.empty()) u.cell_ptr.push_back(0);
+    for (int c = 0; c < p.n_cells; ++c) u.cell_ptr.push_back(p.cell_ptr[c + 1] + ot);
+    for (int v : p.cell_faces) u.cell_faces.push_back(v + of);
+    for (int v : p.cell_nb) u.cell_nb.push_back(v + oc);
+    cat(u.cell_dof, p.cell_dof);
+    cat(u.cell_eta0c, p.cell_eta0c);
+    cat(u.cell_ctr, p.cell_ctr);
+    cat(u.cell_vol, p.cell_vol);
+    cat(u.cell_face_ctr, p.cell_face_ctr);
+    for (int v : p.inner) u.inner.push_back(v + oc);
+    for (int v : p.bond1) u.bond1.push_back(v + oc);
+    for (int v : p.bond2) u.bond2.push_back(v + oc);
+    for (int z = 0; z < p.n_zones(); ++z) {
+      u.zone.push_back(zid++);
+      u.zone.push_back(p.zone[4 * z + 1] + of);
+      u.zone.push_back(p.zone[4 * z + 2] + of);
+      u.zone.push_back(p.zone[4 * z + 3]);
+    }
+    u.face_case.insert(u.face_case.end(), p.n_faces, (int)k);
+    u.n_nodes += p.n_nodes;
+    u.n_cells += p.n_cells;
+    u.n_faces += p.n_faces;
+    u.case_cells.push_back(u.n_cells);
+  }
+  if ((long)parts.size() >= (1L << (31 - kInfoCaseShift))) {
+    *err = "too many cases in one batch";
+    return kEInval;
+  }
+  // every interior face is interpolated in the corrected face-value rule
+  u.n_int_faces = u.n_faces;
   return kOk;
 }
 

@@ -38,6 +38,9 @@ struct HostMesh {
   std::vector<double> cell_dof, cell_eta0c, cell_ctr, cell_vol;
   std::vector<double> cell_face_ctr;    // [tot][2] face centre in cell frame
   std::vector<int> inner, bond1, bond2;
+  // batches of independent cases (empty for one mesh): the case of every
+  // face, and the first file cell of every case plus the end [n_cases+1]
+  std::vector<int> face_case, case_cells;
   bool periodic() const { return !c1_shift.empty(); }
   int n_zones() const { return (int)zone.size() / 4; }
 };
@@ -52,6 +55,12 @@ int build_from_arrays(int n_nodes, const double* node_xy, int n_cells,
                       const double* c1_shift, HostMesh* m, std::string* err);
 // Geometry + derived connectivity; called by both builders.
 int build_geometry(HostMesh* m, std::string* err);
+// Disjoint union of independent meshes (a batch of cases): nodes, cells and
+// faces of part k follow those of parts 0..k-1, with every id shifted; the
+// geometry is copied, not recomputed; face_case / case_cells record the
+// parts.  Only the corrected (quirk-free) face-value rule applies to a union.
+int build_union(const std::vector<const HostMesh*>& parts, HostMesh* out,
+                std::string* err);
 
 // ---------------------------------------------------------------------------
 // Device layout.  Cells are renumbered along a Morton curve of their
@@ -75,6 +84,7 @@ enum FaceKind : int {
 // f_info bits: [0,3) kind, 3/4 reference flags (axis 0/1), 5/6 geometric flags
 constexpr int kInfoFlagRef = 3;
 constexpr int kInfoFlagGeo = 5;
+constexpr int kInfoCaseShift = 8;  // batch case id of the face (bits 8..30)
 
 // per-cell-face gradient record: cf_nb low 29 bits = neighbour device cell,
 // top bits = face-value mode

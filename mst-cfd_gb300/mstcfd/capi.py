@@ -40,6 +40,27 @@ class MeshDesc(C.Structure):
                 ("n_zones", C.c_int), ("zones", _ip), ("c1_shift", _dp)]
 
 
+class CaseParams(C.Structure):
+    _fields_ = [("inlet_q", C.c_double * 4), ("mu", C.c_double), ("lambda_", C.c_double),
+                ("kappa", C.c_double), ("cv", C.c_double)]
+
+
+class ImplicitParams(C.Structure):
+    _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double),
+                ("tol", C.c_double), ("max_iter", C.c_int), ("graph_iters", C.c_int),
+                ("autotune", C.c_int), ("reserved", C.c_int * 5)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_cases", C.c_int), ("n_cells", C.c_int), ("n_faces", C.c_int),
+                ("n_colors", C.c_int), ("sweep_threads", C.c_int), ("graph_iters", C.c_int)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("total_iterations", C.c_int),
+                ("n_converged", C.c_int), ("ms", C.c_double)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [(n, C.c_int) for n in (
         "n_nodes", "n_cells", "n_faces", "n_int_faces", "n_zones",
@@ -127,6 +148,18 @@ def load():
         "mst_read_cell_text": (C.c_int, [C.c_void_p, C.c_char_p]),
         "mst_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p]),
         "mst_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "mst_implicit_params_default": (None, [C.POINTER(ImplicitParams)]),
+        "mst_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(CaseParams), C.c_int,
+                                       C.POINTER(Params), C.POINTER(ImplicitParams),
+                                       C.POINTER(C.c_void_p)]),
+        "mst_batch_destroy": (C.c_int, [C.c_void_p]),
+        "mst_batch_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
+        "mst_batch_colors": (C.c_int, [C.c_void_p, _ip]),
+        "mst_batch_set_state": (C.c_int, [C.c_void_p, _dp]),
+        "mst_batch_get_state": (C.c_int, [C.c_void_p, _dp]),
+        "mst_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
+        "mst_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(BatchResult)]),
+        "mst_batch_case_status": (C.c_int, [C.c_void_p, _ip, _dp, _dp]),
         "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
                                     C.POINTER(C.c_void_p)]),
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),

@@ -110,9 +110,10 @@ def _edges_from_tris(tri_nodes, tri_xy):
     return e, owner, key
 
 
-def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
-            left=INLET, right=OUTLET, bottom=WALL, top=SYMMETRY):
-    """Jittered Delaunay triangles on a box, one boundary zone per side."""
+def _box_triangulation(nx, ny, lx, ly, jitter, seed):
+    """Jittered Delaunay triangles on [0,lx]x[0,ly]: points, triangles,
+    unique edges with their cells, and the box side of each boundary edge
+    (0 left, 1 right, 2 bottom, 3 top)."""
     from scipy.spatial import Delaunay
     rng = np.random.default_rng(seed)
     hx, hy = lx / nx, ly / ny
@@ -126,7 +127,6 @@ def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
     a, b, c = pts[tri[:, 0]], pts[tri[:, 1]], pts[tri[:, 2]]
     area = 0.5 * ((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
     tri = tri[np.abs(area) > 1e-14 * hx * hy]
-    cen = pts[tri].mean(1)
     e, owner, key = _edges_from_tris(tri, pts)
     k = key[:, 0] * len(pts) + key[:, 1]
     order = np.argsort(k, kind="stable")
@@ -153,19 +153,66 @@ def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
     side[~interior & (np.abs(mid[:, 1] - ly) < tol * ly)] = 3
     if np.any(~interior & (side < 0)):
         raise RuntimeError("boundary edge off the box")
-    kinds = [left, right, bottom, top]
-    sel = [np.where(interior)[0]] + [np.where(side == s)[0] for s in range(4)]
-    faces = np.concatenate([en[s] for s in sel]).astype(np.int32)
-    fc = np.stack([np.concatenate([c0[s] for s in sel]),
-                   np.concatenate([c1[s] for s in sel])], 1).astype(np.int32)
+    return pts, tri, en, c0, c1, interior, side, mid
+
+
+def _assemble(pts, tri, en, c0, c1, groups):
+    """Faces in zone order: groups = [(edge indices, zone type)], interior
+    first; area vectors oriented into c0."""
+    faces = np.concatenate([en[s] for s, _ in groups]).astype(np.int32)
+    fc = np.stack([np.concatenate([c0[s] for s, _ in groups]),
+                   np.concatenate([c1[s] for s, _ in groups])], 1).astype(np.int32)
     zones, start = [], 1
-    for zi, (s, ty) in enumerate(zip(sel, [INTERIOR] + kinds)):
+    for zi, (s, ty) in enumerate(groups):
         zones.append((zi + 1, start, start + len(s) - 1, ty))
         start += len(s)
     zones = [z for z in zones if z[2] >= z[1]]
+    cen = pts[tri].mean(1)
     fn = _orient_into_c0(pts, faces, fc, cen[fc[:, 0]])
     return dict(node_xy=pts, face_nodes=fn, face_cells=fc,
                 zones=np.array(zones, np.int32), n_cells=len(tri))
+
+
+def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
+            left=INLET, right=OUTLET, bottom=WALL, top=SYMMETRY):
+    """Jittered Delaunay triangles on a box, one boundary zone per side."""
+    pts, tri, en, c0, c1, interior, side, _ = _box_triangulation(nx, ny, lx, ly, jitter, seed)
+    groups = [(np.where(interior)[0], INTERIOR)]
+    groups += [(np.where(side == s)[0], ty) for s, ty in enumerate([left, right, bottom, top])]
+    return _assemble(pts, tri, en, c0, c1, groups)
+
+
+def wedge(cells=20000, angle_deg=10.0, seed=1, length=3.0, height=1.5, ramp_x=0.5,
+          jitter=0.2):
+    """Supersonic compression ramp: the box [0,length]x[0,height] whose floor
+    turns up by angle_deg at x = ramp_x, triangulated with about `cells`
+    jittered Delaunay triangles (the triangulation of the box, mapped so
+    the floor follows the ramp).  Zones: inlet (left), outlet (right and
+    top), symmetry (floor before the ramp), wall (the ramp)."""
+    ny = max(4, int(round(np.sqrt(cells * height / (2.0 * length)))))
+    nx = max(4, int(round(cells / (2.0 * ny))))
+    pts, tri, en, c0, c1, interior, side, mid = _box_triangulation(nx, ny, length, height,
+                                                                   jitter, seed)
+    t = np.tan(np.radians(angle_deg))
+    x, y = pts[:, 0], pts[:, 1]
+    yw = np.maximum(0.0, x - ramp_x) * t
+    pts = np.stack([x, yw + y * (height - yw) / height], 1)
+    floor = side == 2
+    groups = [(np.where(interior)[0], INTERIOR),
+              (np.where(side == 0)[0], INLET),
+              (np.where(floor & (mid[:, 0] < ramp_x))[0], SYMMETRY),
+              (np.where(floor & (mid[:, 0] >= ramp_x))[0], WALL),
+              (np.where((side == 1) | (side == 3))[0], OUTLET)]
+    return _assemble(pts, tri, en, c0, c1, groups)
+
+
+def freestream(mach, n=None, angle_deg=0.0):
+    """Free-stream conserved state, rho = 1, p = 1/gamma (speed of sound 1),
+    velocity mach along angle_deg; one row, or n rows."""
+    a = np.radians(angle_deg)
+    q = primitive_to_q(np.array([1.0]), np.array([mach * np.cos(a)]),
+                       np.array([mach * np.sin(a)]), np.array([1.0 / GAMMA]))[0]
+    return q if n is None else np.tile(q, (n, 1))
 
 
 def periodic_delaunay(n=1000, length=10.0, jitter=0.25, seed=20261203):

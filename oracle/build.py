@@ -15,7 +15,8 @@ LIB = os.path.join(BUILD, "libmstoracle.so")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_SRC = os.environ.get("MSTCFD_REF_SRC", "/root/reference/MST-CFD")
 
-_SOURCES = ["mstoracle.c", "mstoracle_ext.c", "mstoracle_lu.c", "mstoracle_io.c"]
+_SOURCES = ["mstoracle.c", "mstoracle_ext.c", "mstoracle_lu.c", "mstoracle_io.c",
+            "mstoracle_implicit.c"]
 
 
 def _stale(target, deps):

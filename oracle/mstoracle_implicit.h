@@ -1,0 +1,27 @@
+/* Implicit steady iterations of the oracle (TEST INFRASTRUCTURE ONLY; see
+ * mstoracle.h and mstoracle_implicit.c). */
+#ifndef MSTORACLE_IMPLICIT_H
+#define MSTORACLE_IMPLICIT_H
+#include "mstoracle.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct om_lusgs_params {
+  double cfl0, cfl_max, omega;
+} om_lusgs_params;
+
+/* niter LU-SGS iterations of one case in place (corrected-mode residual of
+ * p, which must have quirks = 0); color [n_cells] the colour of each cell;
+ * l2_hist [niter] (nullable) the L2 of R_rho / V before each update. */
+int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
+                     const int *color, const om_lusgs_params *ip, int niter,
+                     double *l2_hist);
+/* Greedy colouring of the cell adjacency in file order; returns the count. */
+int om_greedy_colors(const om_mesh *m, int *color);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

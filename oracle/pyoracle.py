@@ -46,6 +46,10 @@ class _OParamsExt(C.Structure):
                 ("lam", C.c_double), ("kappa", C.c_double), ("cv", C.c_double)]
 
 
+class _OLusgs(C.Structure):
+    _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double)]
+
+
 class _ONorms(C.Structure):
     _fields_ = [("linf", C.c_double * 4), ("l2", C.c_double * 4),
                 ("mass", C.c_double), ("dt", C.c_double), ("time", C.c_double)]
@@ -93,6 +97,9 @@ def lib():
         L.om_cell_nodes.argtypes = [C.POINTER(_OMesh), _ip, _ip]
         L.om_write_plt.argtypes = [C.POINTER(_OMesh), _dp, C.c_double, C.c_int, C.c_char_p]
         L.om_write_cell_text.argtypes = [C.c_int, _dp, C.c_char_p]
+        L.om_lusgs_iterate.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParamsExt), _dp, _ip,
+                                       C.POINTER(_OLusgs), C.c_int, _dp]
+        L.om_greedy_colors.argtypes = [C.POINTER(_OMesh), _ip]
         _lib = L
     return _lib
 
@@ -354,3 +361,25 @@ def write_cell_text(q, path):
     rc = lib().om_write_cell_text(len(q), _d(q), os.fsencode(path))
     if rc != 0:
         raise ValueError(f"oracle: cannot write {path} (status {rc})")
+
+
+# ---------------------------------------------------------------------------
+# implicit steady iterations (mstoracle_implicit.c)
+# ---------------------------------------------------------------------------
+def greedy_colors(mesh):
+    col = np.zeros(mesh.n_cells, np.int32)
+    n = lib().om_greedy_colors(mesh._p, _i(col))
+    return col, n
+
+
+def lusgs_iterate(mesh, prm, q, color, niter, cfl0=5.0, cfl_max=200.0, omega=1.5):
+    """niter LU-SGS iterations from q; returns (q, L2 history)."""
+    q = _f64(q).copy()
+    col = np.ascontiguousarray(color, dtype=np.int32)
+    ip = _OLusgs(float(cfl0), float(cfl_max), float(omega))
+    hist = np.zeros(max(int(niter), 1))
+    rc = lib().om_lusgs_iterate(mesh._p, C.byref(prm), _d(q), _i(col), C.byref(ip),
+                                int(niter), _d(hist))
+    if rc != 0:
+        raise ValueError(f"oracle: lusgs failed (status {rc})")
+    return q, hist[:int(niter)]

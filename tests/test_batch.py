@@ -1,0 +1,176 @@
+"""Batched steady solves (implicit LU-SGS over colour groups).
+
+* oracle: the greedy colouring is a proper colouring; LU-SGS on an inviscid
+  compression ramp converges to round-off and gives the oblique-shock
+  density ratio of the theta-beta-Mach relation;
+* GPU (through the C ABI): per case bit-identical to the oracle's
+  iterations (FP64-exact, constant CFL), inviscid and viscous, for a batch
+  of cases of different sizes and inflow states; colours equal the
+  oracle's; mst_batch_solve (CUDA graph) reaches the tolerance and
+  repeats bit-for-bit the plain iterations; the FP64 production path and
+  the FP32 residual agree with the exact path to their rounding.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+GAMMA = 1.4
+CV = 1.0 / (GAMMA * (GAMMA - 1.0))
+
+
+def _wedge(cells, angle, seed):
+    from mstcfd import meshgen as mg
+    return mg.wedge(cells, angle, seed=seed)
+
+
+def _oracle_mesh(m):
+    return po.mesh_from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                               m["n_cells"])
+
+
+def _visc(mach, re):
+    mu = mach / re
+    return mu, -2.0 / 3.0 * mu, mu * GAMMA * CV / 0.72
+
+
+def test_oracle_colors_are_proper():
+    m = _wedge(3000, 12.0, 4)
+    om = _oracle_mesh(m)
+    col, n = po.greedy_colors(om)
+    assert 2 <= n <= 4
+    fc = om.face_cells[om.face_cells[:, 1] >= 0]
+    assert np.all(col[fc[:, 0]] != col[fc[:, 1]])
+
+
+def _beta(mach, theta):
+    """Weak oblique-shock angle of the theta-beta-Mach relation."""
+    from scipy.optimize import brentq
+    t = np.radians(theta)
+    f = lambda b: (2 / np.tan(b) * (mach ** 2 * np.sin(b) ** 2 - 1)
+                   / (mach ** 2 * (GAMMA + np.cos(2 * b)) + 2)) - np.tan(t)
+    mu = np.arcsin(1 / mach)
+    return brentq(f, mu + 1e-6, np.radians(64.0))
+
+
+def test_oracle_lusgs_inviscid_ramp_converges_to_oblique_shock():
+    from mstcfd import meshgen as mg
+    mach, theta = 2.0, 10.0
+    m = _wedge(3000, theta, 1)
+    om = _oracle_mesh(m)
+    prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=mg.freestream(mach))
+    col, _ = po.greedy_colors(om)
+    q, hist = po.lusgs_iterate(om, prm, mg.freestream(mach, om.n_cells), col, 700,
+                               cfl0=50.0, cfl_max=5000.0, omega=1.2)
+    assert hist[-1] / hist[0] < 1e-10
+    b = _beta(mach, theta)
+    mn = mach * np.sin(b)
+    ratio = (GAMMA + 1) * mn ** 2 / ((GAMMA - 1) * mn ** 2 + 2)
+    # cells well behind the shock and away from the outlet corner
+    x, y = om.cell_ctr[:, 0], om.cell_ctr[:, 1]
+    xr = 0.5
+    yw = (x - xr) * np.tan(np.radians(theta))
+    ys = (x - xr) * np.tan(b)
+    sel = (x > 1.2) & (x < 2.2) & (y > yw + 0.05) & (y < yw + 0.5 * (ys - yw))
+    assert sel.sum() > 20
+    assert abs(np.median(q[sel, 0]) - ratio) < 0.02 * ratio
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+SPECS = [(1500, 8.0, 1.8, 3), (2600, 12.0, 2.4, 5), (2000, 6.0, 2.9, 7)]
+
+
+def _batch_cases(viscous, specs=SPECS):
+    from mstcfd import Mesh, batch
+    from mstcfd import meshgen as mg
+    out = []
+    for cells, angle, mach, seed in specs:
+        m = _wedge(cells, angle, seed)
+        mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                                m["n_cells"])
+        mu, lam, kap = _visc(mach, 2000.0 + 1000 * seed) if viscous else (0.0, 0.0, 0.0)
+        out.append((m, mesh, mach,
+                    batch.case_params(mg.freestream(mach), mu=mu, lambda_=lam, kappa=kap, cv=CV)))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("viscous", [0, 1], ids=["euler", "laminar"])
+def test_gpu_batch_matches_oracle(viscous):
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(viscous)
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                    implicit=dict(cfl0=40.0, cfl_max=40.0, omega=1.2, autotune=0,
+                                  graph_iters=0),
+                    flux=1, order=2, limiter=1, precision=0, viscous=viscous)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    b.set_state(q0)
+    b.iterate(12)
+    got = b.state()
+    cols = b.colors()
+    st = b.case_status()
+    for k, (m, mesh, mach, cp) in enumerate(cases):
+        om = _oracle_mesh(m)
+        col, _ = po.greedy_colors(om)
+        assert np.array_equal(cols[k], col)
+        prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=cp["inlet_q"], viscous=viscous,
+                            mu=cp["mu"], lam=cp["lambda_"], kappa=cp["kappa"], cv=cp["cv"])
+        q, hist = po.lusgs_iterate(om, prm, q0[k], col, 12, cfl0=40.0, cfl_max=40.0, omega=1.2)
+        assert np.array_equal(got[k], q), k
+        assert np.isclose(st["first_l2"][k], hist[0], rtol=1e-12)
+        assert np.isclose(st["last_l2"][k], hist[-1], rtol=1e-12)
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_batch_solve_converges_and_graph_is_deterministic():
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    imp = dict(cfl0=50.0, cfl_max=5000.0, omega=1.2, tol=1e-8, max_iter=3000)
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                    implicit=dict(imp, graph_iters=10), **kw)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    b.set_state(q0)
+    r = b.solve()
+    assert r["n_converged"] == len(cases)
+    st = b.case_status()
+    assert np.all(st["conv_iter"] > 0)
+    assert np.all(st["last_l2"] <= 1e-8 * st["first_l2"] * 1.0001)
+    info = b.info()
+    assert info["graph_iters"] == 10 and info["sweep_threads"] in (64, 128, 256)
+    # the same number of plain iterations repeats the graph's result exactly
+    b2 = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                     implicit=dict(imp, graph_iters=0, autotune=0), **kw)
+    b2.set_state(q0)
+    b2.iterate(r["iterations"])
+    for a, c in zip(b.state(), b2.state()):
+        assert np.array_equal(a, c)
+    b.close()
+    b2.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [1, 2], ids=["fp64", "fp32"])
+def test_gpu_batch_production_precisions_track_exact(prec):
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    out = {}
+    for p in (0, prec):
+        b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                        implicit=dict(cfl0=40.0, cfl_max=40.0, omega=1.2, autotune=0,
+                                      graph_iters=0),
+                        flux=1, order=2, limiter=1, precision=p)
+        b.set_state(q0)
+        b.iterate(30)
+        out[p] = b.state()
+        b.close()
+    tol = 1e-9 if prec == 1 else 2e-4
+    for a, c in zip(out[0], out[prec]):
+        assert np.abs(a - c).max() <= tol * np.abs(a).max()
