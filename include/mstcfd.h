@@ -257,15 +257,22 @@ typedef struct mst_implicit_params {
   double cfl0;      /* CFL of the first iteration */
   double cfl_max;   /* ceiling of CFL = cfl0 * L2_first / L2 */
   double omega;     /* LU-SGS relaxation of the spectral radii (>= 1) */
-  double tol;       /* a case has converged when L2 <= tol * L2_first */
+  double tol;       /* a case has converged when L2 <= tol * L2_first; its
+                     * state is kept from then on */
+  /* limiter freezing: the iteration after a case's L2 first falls to
+   * freeze_tol * L2_first records the ratio slope / (upwind difference) of
+   * every limited face side; later iterations reconstruct with those
+   * ratios times the current upwind differences, so
+   * the limiter's switching no longer stalls convergence (0: never) */
+  double freeze_tol;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
   int autotune;     /* time the sweep block sizes once and keep the fastest */
   int reserved[5];
 } mst_implicit_params;
 
-/* cfl0 5, cfl_max 200, omega 1.5, tol 1e-8, max_iter 20000,
- * graph_iters 20, autotune on. */
+/* cfl0 50, cfl_max 1000, omega 1.2, tol 1e-8, freeze_tol 1e-2,
+ * max_iter 20000, graph_iters 20, autotune on. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {

@@ -40,11 +40,12 @@ __global__ void k_batch_gather(const double4_32a* __restrict__ src,
   if (i < n) dst[i] = src[idx[i]];
 }
 __global__ void k_batch_reset(int n_cases, double cfl0, double* cfl, int* conv_iter,
-                              int* n_conv, int* iter) {
+                              int* frozen, int* n_conv, int* iter) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_cases) {
     cfl[i] = cfl0;
     conv_iter[i] = -1;
+    frozen[i] = 0;
   }
   if (i == 0) {
     *n_conv = 0;
@@ -71,6 +72,8 @@ struct mst_batch {
   float* case_tab_f = nullptr;
   double *cfl = nullptr, *first = nullptr, *last = nullptr;
   int *conv_iter = nullptr, *n_conv = nullptr, *iter = nullptr;
+  int* frozen = nullptr;         // per-case limiter-freezing state
+  void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
@@ -132,6 +135,10 @@ mst_status enqueue_residual(mst_batch* b, int which) {
   mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa, c->p.cv);
   a.case_tab = b->case_tab;
   a.case_tab_f = b->case_tab_f;
+  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE) {
+    a.case_frozen = b->frozen;
+    a.phi = b->phi;
+  }
   e = exact(b) ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
                : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
   if (e != cudaSuccess)
@@ -155,6 +162,7 @@ mst::LusgsArgs sweep_args(mst_batch* b, int which) {
   la.mu = c->p.mu;
   la.viscous = c->p.viscous;
   la.omega = b->ip.omega;
+  la.conv_iter = b->conv_iter;
   return la;
 }
 
@@ -194,6 +202,8 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.conv_iter = b->conv_iter;
   na.n_conv = b->n_conv;
   na.iter = b->iter;
+  na.frozen = b->ip.freeze_tol > 0 ? b->frozen : nullptr;
+  na.freeze_tol = b->ip.freeze_tol;
   na.cfl0 = b->ip.cfl0;
   na.cfl_max = b->ip.cfl_max;
   na.tol = b->ip.tol;
@@ -271,7 +281,7 @@ mst_status build_graph(mst_batch* b, int k) {
 
 mst_status reset_progress(mst_batch* b) {
   k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, b->ctx->stream>>>(
-      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->n_conv, b->iter);
+      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->frozen, b->n_conv, b->iter);
   B_CU(cudaGetLastError());
   return MST_OK;
 }
@@ -292,10 +302,11 @@ extern "C" {
 void mst_implicit_params_default(mst_implicit_params* p) {
   if (!p) return;
   std::memset(p, 0, sizeof *p);
-  p->cfl0 = 5.0;
-  p->cfl_max = 200.0;
-  p->omega = 1.5;
+  p->cfl0 = 50.0;
+  p->cfl_max = 1000.0;
+  p->omega = 1.2;
   p->tol = 1e-8;
+  p->freeze_tol = 1e-2;
   p->max_iter = 20000;
   p->graph_iters = 20;
   p->autotune = 1;
@@ -310,6 +321,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
   if (p->reference_quirks)
     return mst_internal_fail(MST_EINVAL, "batches run the corrected scheme (reference_quirks = 0)");
   if (!(ip->cfl0 > 0) || !(ip->cfl_max >= ip->cfl0) || !(ip->omega >= 1.0) || !(ip->tol > 0) ||
+      !(ip->freeze_tol >= 0) ||
       ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1))
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
@@ -396,6 +408,10 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->conv_iter, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->n_conv, sizeof(int))) ||
       (st = balloc(b.get(), &b->iter, sizeof(int))) ||
+      (st = balloc(b.get(), &b->frozen, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->phi,
+                   (size_t)8 * h.n_faces *
+                       (p->precision == MST_PREC_FP32 ? sizeof(float) : sizeof(double)))) ||
       (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
       (st = reset_progress(b.get()))) {

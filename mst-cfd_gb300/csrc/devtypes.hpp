@@ -75,6 +75,11 @@ struct StepArgs {
   // for a single case (the scalars above)
   const double* case_tab;
   const float* case_tab_f;
+  // limiter freezing (residual-only launches of the implicit path): per
+  // case 0 live, 1 record the ratios slope / (upwind difference) of every
+  // limited face into phi [n_faces][2][4] (path precision), 2 use them
+  const int* case_frozen;
+  void* phi;
   double* partials;       // [n_tiles][kNormSlots] or nullptr
 };
 constexpr int kCaseWords = 8;
@@ -115,6 +120,7 @@ struct LusgsArgs {
   double mu;               // viscosity of a single case
   int viscous;
   double omega;
+  const int* conv_iter;    // [n_cases] converged cases keep their state
 };
 
 // Per-case residual norms and the CFL of the next iteration, one block per
@@ -132,7 +138,8 @@ struct CaseNormArgs {
   int* conv_iter;          // [n_cases] -1 until converged
   int* n_conv;             // number of converged cases
   int* iter;               // iteration counter (advanced by k_iter_advance)
-  double cfl0, cfl_max, tol;
+  int* frozen;             // [n_cases] limiter-freezing state (or nullptr)
+  double cfl0, cfl_max, tol, freeze_tol;
 };
 
 // Precisions / schemes (mirrors of the public enums)

@@ -143,6 +143,11 @@ typedef struct om_params_ext {
   double inlet_q[4];
   int viscous;      /* laminar viscous term (order 2) */
   double mu, lam, kappa, cv;
+  /* limiter freezing (limited 2nd order): phi [n_faces][2][4] the ratios
+   * slope / (upwind difference) of each face side; phi_mode 0 off,
+   * 1 record, 2 use (times the current upwind difference) */
+  double *phi;
+  int phi_mode;
 } om_params_ext;
 
 typedef struct om_norms {

@@ -171,12 +171,26 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
             recon_e(q1, g1, r1x, r1y, R);
           } else {
             const double dx = r0x - r1x, dy = r0y - r1y;
+            double *ph = p->phi ? p->phi + 8 * (size_t)i : NULL;
             for (int k = 0; k < 4; ++k) {
               const double dc = q1[k] - q0[k];
               const double du0 = 2.0 * (g0[k] * dx + g0[4 + k] * dy) - dc;
               const double du1 = 2.0 * (g1[k] * dx + g1[4 + k] * dy) - dc;
-              L[k] = q0[k] + 0.5 * slope_e(p->limiter, du0, dc);
-              R[k] = q1[k] - 0.5 * slope_e(p->limiter, du1, dc);
+              if (ph && p->phi_mode == 2) {
+                /* frozen limiter: the recorded ratios times the current
+                 * upwind differences (a smooth reconstruction) */
+                L[k] = q0[k] + 0.5 * (ph[k] * du0);
+                R[k] = q1[k] - 0.5 * (ph[4 + k] * du1);
+                continue;
+              }
+              const double s0 = slope_e(p->limiter, du0, dc);
+              const double s1 = slope_e(p->limiter, du1, dc);
+              L[k] = q0[k] + 0.5 * s0;
+              R[k] = q1[k] - 0.5 * s1;
+              if (ph && p->phi_mode == 1) {
+                ph[k] = du0 != 0.0 ? s0 / du0 : 0.0;
+                ph[4 + k] = du1 != 0.0 ? s1 / du1 : 0.0;
+              }
             }
           }
         }

@@ -107,10 +107,19 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
     return OM_EINVAL;
   }
   for (c = 0; c < nC; ++c) ncol = color[c] + 1 > ncol ? color[c] + 1 : ncol;
+  om_params_ext pp = *p;
+  double *phi = NULL;
+  int frozen = 0; /* 0 live limiter, 1 record this iteration, 2 frozen */
+  int converged = 0;
+  if (ip->freeze_tol > 0) {
+    phi = (double *)calloc((size_t)8 * (m->n_faces > 0 ? m->n_faces : 1), 8);
+    pp.phi = phi;
+  }
   for (it = 0; it < niter; ++it) {
     double s = 0.0, l2;
+    pp.phi_mode = phi ? frozen : 0;
     if (p->order == 2) om_gradient_ext(m, q, 0, grad);
-    om_face_flux_ext(m, p, q, p->order == 2 ? grad : NULL, F);
+    om_face_flux_ext(m, &pp, q, p->order == 2 ? grad : NULL, F);
     om_gather(m, F, R);
     for (c = 0; c < nC; ++c) {
       const double x = R[4 * (size_t)c] / m->cell_vol[c];
@@ -119,6 +128,12 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
     l2 = sqrt(s / (double)(nC > 0 ? nC : 1));
     if (it == 0) first = l2;
     if (l2_hist) l2_hist[it] = l2;
+    /* limiter freezing: the iteration after the case first falls below
+     * freeze_tol records the limiter ratios, later ones reuse them */
+    if (frozen == 1) frozen = 2;
+    else if (phi && frozen == 0 && first > 0.0 && l2 <= ip->freeze_tol * first) frozen = 1;
+    if (!converged && ip->tol > 0 && first > 0.0 && l2 <= ip->tol * first) converged = 1;
+    if (converged) continue; /* the state that met the tolerance is kept */
     /* the CFL of this iteration from the norms of this residual */
     cfl = ip->cfl0;
     if (l2 > 0.0 && first > 0.0) cfl = ip->cfl0 * (first / l2);
@@ -147,7 +162,7 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
       }
     memcpy(q, qn, sizeof(double) * 4 * (size_t)nC);
   }
-  free(F), free(grad), free(R), free(dq), free(D), free(qn);
+  free(F), free(grad), free(R), free(dq), free(D), free(qn), free(phi);
   return OM_OK;
 }
 

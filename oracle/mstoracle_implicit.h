@@ -10,6 +10,13 @@ extern "C" {
 
 typedef struct om_lusgs_params {
   double cfl0, cfl_max, omega;
+  /* limiter freezing: the iteration after L2 first falls to freeze_tol *
+   * L2_first records the limiter ratios slope / (upwind difference) of
+   * every face, later iterations reuse them (0: never) */
+  double freeze_tol;
+  /* convergence: from the first iteration with L2 <= tol * L2_first on,
+   * the state is kept (0: never) */
+  double tol;
 } om_lusgs_params;
 
 /* niter LU-SGS iterations of one case in place (corrected-mode residual of

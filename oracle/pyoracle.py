@@ -43,11 +43,13 @@ class _OParamsExt(C.Structure):
                 ("quirks", C.c_int), ("rk2", C.c_int), ("dt_mode", C.c_int),
                 ("dt", C.c_double), ("cfl", C.c_double),
                 ("inlet_q", C.c_double * 4), ("viscous", C.c_int), ("mu", C.c_double),
-                ("lam", C.c_double), ("kappa", C.c_double), ("cv", C.c_double)]
+                ("lam", C.c_double), ("kappa", C.c_double), ("cv", C.c_double),
+                ("phi", _dp), ("phi_mode", C.c_int)]
 
 
 class _OLusgs(C.Structure):
-    _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double)]
+    _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double),
+                ("freeze_tol", C.c_double), ("tol", C.c_double)]
 
 
 class _ONorms(C.Structure):
@@ -372,11 +374,12 @@ def greedy_colors(mesh):
     return col, n
 
 
-def lusgs_iterate(mesh, prm, q, color, niter, cfl0=5.0, cfl_max=200.0, omega=1.5):
+def lusgs_iterate(mesh, prm, q, color, niter, cfl0=5.0, cfl_max=200.0, omega=1.5,
+                  freeze_tol=0.0, tol=0.0):
     """niter LU-SGS iterations from q; returns (q, L2 history)."""
     q = _f64(q).copy()
     col = np.ascontiguousarray(color, dtype=np.int32)
-    ip = _OLusgs(float(cfl0), float(cfl_max), float(omega))
+    ip = _OLusgs(float(cfl0), float(cfl_max), float(omega), float(freeze_tol), float(tol))
     hist = np.zeros(max(int(niter), 1))
     rc = lib().om_lusgs_iterate(mesh._p, C.byref(prm), _d(q), _i(col), C.byref(ip),
                                 int(niter), _d(hist))

@@ -96,15 +96,39 @@ def _batch_cases(viscous, specs=SPECS):
     return out
 
 
+SPECS_STALL = [(1500, 8.0, 1.8, 3), (2600, 12.0, 2.4, 5), (2000, 6.0, 2.9, 7)]
+
+
+@pytest.mark.parametrize("freeze", [0.0, 1e-2])
+def test_oracle_limiter_freezing_removes_the_stall(freeze):
+    """Minmod's switching stalls LU-SGS on two of these ramps; with the
+    limiter frozen at 1e-2 every case reaches 1e-8."""
+    from mstcfd import meshgen as mg
+    conv = []
+    for cells, angle, mach, seed in SPECS_STALL:
+        om = _oracle_mesh(_wedge(cells, angle, seed))
+        prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=mg.freestream(mach))
+        col, _ = po.greedy_colors(om)
+        _, h = po.lusgs_iterate(om, prm, mg.freestream(mach, om.n_cells), col, 1000,
+                                cfl0=50.0, cfl_max=1000.0, omega=1.2, freeze_tol=freeze,
+                                tol=1e-8)
+        conv.append(h[-1] / h[0] < 1e-8)
+    if freeze:
+        assert all(conv)
+    else:
+        assert not all(conv)
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("freeze", [0.0, 0.9], ids=["live", "frozen"])
 @pytest.mark.parametrize("viscous", [0, 1], ids=["euler", "laminar"])
-def test_gpu_batch_matches_oracle(viscous):
+def test_gpu_batch_matches_oracle(viscous, freeze):
     from mstcfd import batch
     from mstcfd import meshgen as mg
     cases = _batch_cases(viscous)
     b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
                     implicit=dict(cfl0=40.0, cfl_max=40.0, omega=1.2, autotune=0,
-                                  graph_iters=0),
+                                  graph_iters=0, freeze_tol=freeze),
                     flux=1, order=2, limiter=1, precision=0, viscous=viscous)
     q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
     b.set_state(q0)
@@ -118,7 +142,8 @@ def test_gpu_batch_matches_oracle(viscous):
         assert np.array_equal(cols[k], col)
         prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=cp["inlet_q"], viscous=viscous,
                             mu=cp["mu"], lam=cp["lambda_"], kappa=cp["kappa"], cv=cp["cv"])
-        q, hist = po.lusgs_iterate(om, prm, q0[k], col, 12, cfl0=40.0, cfl_max=40.0, omega=1.2)
+        q, hist = po.lusgs_iterate(om, prm, q0[k], col, 12, cfl0=40.0, cfl_max=40.0, omega=1.2,
+                                   freeze_tol=freeze)
         assert np.array_equal(got[k], q), k
         assert np.isclose(st["first_l2"][k], hist[0], rtol=1e-12)
         assert np.isclose(st["last_l2"][k], hist[-1], rtol=1e-12)
@@ -131,7 +156,7 @@ def test_gpu_batch_solve_converges_and_graph_is_deterministic():
     from mstcfd import meshgen as mg
     cases = _batch_cases(0)
     kw = dict(flux=1, order=2, limiter=1, precision=1)
-    imp = dict(cfl0=50.0, cfl_max=5000.0, omega=1.2, tol=1e-8, max_iter=3000)
+    imp = dict(cfl0=50.0, cfl_max=1000.0, omega=1.2, tol=1e-8, freeze_tol=1e-2, max_iter=3000)
     b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
                     implicit=dict(imp, graph_iters=10), **kw)
     q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
@@ -155,6 +180,35 @@ def test_gpu_batch_solve_converges_and_graph_is_deterministic():
 
 
 @pytest.mark.gpu
+def test_gpu_batch_solve_matches_oracle_solve():
+    """FP64-exact batch solved to 1e-8 with limiter freezing: every case's
+    final state and convergence iteration equal the oracle's single-case
+    run (converged cases keep their state, so the batch composition does
+    not matter)."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    imp = dict(cfl0=50.0, cfl_max=50.0, omega=1.2, tol=1e-8, freeze_tol=1e-2, max_iter=2000)
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=dict(imp, graph_iters=10),
+                    flux=1, order=2, limiter=1, precision=0)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    b.set_state(q0)
+    r = b.solve()
+    st = b.case_status()
+    got = b.state()
+    for k, (m, mesh, mach, cp) in enumerate(cases):
+        om = _oracle_mesh(m)
+        col, _ = po.greedy_colors(om)
+        prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=cp["inlet_q"])
+        q, hist = po.lusgs_iterate(om, prm, q0[k], col, r["iterations"], cfl0=50.0,
+                                   cfl_max=50.0, omega=1.2, freeze_tol=1e-2, tol=1e-8)
+        assert np.array_equal(got[k], q), k
+        conv = np.nonzero(hist <= 1e-8 * hist[0])[0]
+        assert len(conv) and st["conv_iter"][k] == conv[0]
+    b.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("prec", [1, 2], ids=["fp64", "fp32"])
 def test_gpu_batch_production_precisions_track_exact(prec):
     from mstcfd import batch
@@ -165,7 +219,7 @@ def test_gpu_batch_production_precisions_track_exact(prec):
     for p in (0, prec):
         b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
                         implicit=dict(cfl0=40.0, cfl_max=40.0, omega=1.2, autotune=0,
-                                      graph_iters=0),
+                                      graph_iters=0, freeze_tol=0.0),
                         flux=1, order=2, limiter=1, precision=p)
         b.set_state(q0)
         b.iterate(30)
