@@ -259,11 +259,14 @@ typedef struct mst_implicit_params {
   double omega;     /* LU-SGS relaxation of the spectral radii (>= 1) */
   double tol;       /* a case has converged when L2 <= tol * L2_first; its
                      * state is kept from then on */
-  /* limiter freezing: the iteration after a case's L2 first falls to
-   * freeze_tol * L2_first records the ratio slope / (upwind difference) of
-   * every limited face side; later iterations reconstruct with those
-   * ratios times the current upwind differences, so
-   * the limiter's switching no longer stalls convergence (0: never) */
+  /* limiter freezing: once a case is below freeze_tol * L2_first and its L2
+   * fell by less than 30% over the last 50 iterations, the next iteration
+   * records the ratio slope / (upwind difference) of every limited face
+   * side; later iterations reconstruct with those ratios times the current
+   * upwind differences, so the limiter's switching no longer stalls
+   * convergence (0: never).  Every update is halved (at most 6 times, else
+   * dropped) until density and pressure stay above a fifth of their
+   * current values. */
   double freeze_tol;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */

@@ -40,12 +40,13 @@ __global__ void k_batch_gather(const double4_32a* __restrict__ src,
   if (i < n) dst[i] = src[idx[i]];
 }
 __global__ void k_batch_reset(int n_cases, double cfl0, double* cfl, int* conv_iter,
-                              int* frozen, int* n_conv, int* iter) {
+                              int* frozen, double* l2_win, int* n_conv, int* iter) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_cases) {
     cfl[i] = cfl0;
     conv_iter[i] = -1;
     frozen[i] = 0;
+    l2_win[i] = 0.0;
   }
   if (i == 0) {
     *n_conv = 0;
@@ -73,6 +74,7 @@ struct mst_batch {
   double *cfl = nullptr, *first = nullptr, *last = nullptr;
   int *conv_iter = nullptr, *n_conv = nullptr, *iter = nullptr;
   int* frozen = nullptr;         // per-case limiter-freezing state
+  double* l2_win = nullptr;      // per-case L2 at the last freezing check
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
@@ -203,6 +205,7 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.n_conv = b->n_conv;
   na.iter = b->iter;
   na.frozen = b->ip.freeze_tol > 0 ? b->frozen : nullptr;
+  na.l2_win = b->l2_win;
   na.freeze_tol = b->ip.freeze_tol;
   na.cfl0 = b->ip.cfl0;
   na.cfl_max = b->ip.cfl_max;
@@ -281,7 +284,7 @@ mst_status build_graph(mst_batch* b, int k) {
 
 mst_status reset_progress(mst_batch* b) {
   k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, b->ctx->stream>>>(
-      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->frozen, b->n_conv, b->iter);
+      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->frozen, b->l2_win, b->n_conv, b->iter);
   B_CU(cudaGetLastError());
   return MST_OK;
 }
@@ -409,6 +412,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->n_conv, sizeof(int))) ||
       (st = balloc(b.get(), &b->iter, sizeof(int))) ||
       (st = balloc(b.get(), &b->frozen, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->l2_win, sizeof(double) * n_cases)) ||
       (st = balloc(b.get(), &b->phi,
                    (size_t)8 * h.n_faces *
                        (p->precision == MST_PREC_FP32 ? sizeof(float) : sizeof(double)))) ||

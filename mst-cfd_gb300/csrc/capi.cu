@@ -429,8 +429,14 @@ mst_status download_rows(mst_ctx* c, const double4_32a* dev, double* host,
   else
     k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(dev, c->d.cell_perm, c->stage_in, nC);
   CU(cudaGetLastError());
-  CU(cudaMemcpy2DAsync(host, stride * sizeof(double), c->stage_in, 4 * sizeof(double),
-                       4 * sizeof(double), nC, cudaMemcpyDeviceToHost, c->stream));
+  // contiguous rows (stride 4): one linear copy; a pitched copy of 32-byte
+  // rows moves row by row
+  if (stride == 4)
+    CU(cudaMemcpyAsync(host, c->stage_in, (size_t)nC * 4 * sizeof(double),
+                       cudaMemcpyDeviceToHost, c->stream));
+  else
+    CU(cudaMemcpy2DAsync(host, stride * sizeof(double), c->stage_in, 4 * sizeof(double),
+                         4 * sizeof(double), nC, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   return MST_OK;
 }
@@ -603,6 +609,17 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
     CU(up(&d.f_r1_32, as_f2(L.f_r1)));
     CU(up(&d.cf_w32, as_f2(L.cf_w)));
     {
+      std::vector<double> cd(2 * L.cf_face.size());
+      for (size_t k = 0; k < L.cf_face.size(); ++k) {
+        const int fs = L.cf_face[k];
+        const int f = fs < 0 ? ~fs : fs;
+        cd[2 * k] = fs < 0 ? -L.f_dir[2 * (size_t)f] : L.f_dir[2 * (size_t)f];
+        cd[2 * k + 1] = fs < 0 ? -L.f_dir[2 * (size_t)f + 1] : L.f_dir[2 * (size_t)f + 1];
+      }
+      CU(up(&d.cf_dir, as_d2(cd)));
+      CU(up(&d.cf_dir32, as_f2(cd)));
+    }
+    {
       std::vector<double> fe(L.n_faces);
       std::vector<float> fe32(L.n_faces);
       for (int i = 0; i < L.n_faces; ++i) {
@@ -658,6 +675,8 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.cf_nb_fix = d.cf_nb_fix;
   dm.cf_w = d.cf_w;
   dm.cf_w32 = d.cf_w32;
+  dm.cf_dir = d.cf_dir;
+  dm.cf_dir32 = d.cf_dir32;
   dm.t_own_ptr = d.t_own_ptr;
   dm.t_bor_ptr = d.t_bor_ptr;
   dm.t_bor = d.t_bor;
@@ -739,8 +758,12 @@ mst_status mst_set_state(mst_ctx* c, const double* q, size_t stride) {
   if (!c || !q) return fail(MST_EINVAL, "NULL argument");
   if (stride < 4) return fail(MST_EINVAL, "stride must be >= 4 doubles");
   const int nC = c->dm.n_cells;
-  CU(cudaMemcpy2DAsync(c->stage_in, 4 * sizeof(double), q, stride * sizeof(double),
-                       4 * sizeof(double), nC, cudaMemcpyHostToDevice, c->stream));
+  if (stride == 4)
+    CU(cudaMemcpyAsync(c->stage_in, q, (size_t)nC * 4 * sizeof(double), cudaMemcpyHostToDevice,
+                       c->stream));
+  else
+    CU(cudaMemcpy2DAsync(c->stage_in, 4 * sizeof(double), q, stride * sizeof(double),
+                         4 * sizeof(double), nC, cudaMemcpyHostToDevice, c->stream));
   k_gather_rows<<<(nC + 255) / 256, 256, 0, c->stream>>>(c->stage_in, c->d.cell_iperm,
                                                            c->q_old, nC);
   CU(cudaGetLastError());

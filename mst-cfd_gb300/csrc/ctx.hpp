@@ -21,8 +21,10 @@ struct mst_mesh {
 struct DevArrays {
   int2* f_c0c1 = nullptr;
   int* f_info = nullptr;
-  double2 *f_dir = nullptr, *f_r0 = nullptr, *f_r1 = nullptr, *cf_w = nullptr;
-  float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr;
+  double2 *f_dir = nullptr, *f_r0 = nullptr, *f_r1 = nullptr, *cf_w = nullptr,
+          *cf_dir = nullptr;
+  float2 *f_dir32 = nullptr, *f_r0_32 = nullptr, *f_r1_32 = nullptr, *cf_w32 = nullptr,
+         *cf_dir32 = nullptr;
   double* f_eta = nullptr;
   float* f_eta32 = nullptr;
   double* c_vol = nullptr;

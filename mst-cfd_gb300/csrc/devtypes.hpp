@@ -31,6 +31,10 @@ struct DevMesh {
   const int* cf_nb_fix;
   const double2* cf_w;
   const float2* cf_w32;
+  // area vector of every cell-face, pointing out of the cell (the signed
+  // f_dir of cf_face): a contiguous load instead of a gather
+  const double2* cf_dir;
+  const float2* cf_dir32;
   const int* t_own_ptr;
   const int* t_bor_ptr;
   const int* t_bor;
@@ -139,6 +143,7 @@ struct CaseNormArgs {
   int* n_conv;             // number of converged cases
   int* iter;               // iteration counter (advanced by k_iter_advance)
   int* frozen;             // [n_cases] limiter-freezing state (or nullptr)
+  double* l2_win;          // [n_cases] L2 at the last freezing-window check
   double cfl0, cfl_max, tol, freeze_tol;
 };
 

@@ -31,9 +31,13 @@ def kernel_bytes(info, precision, order, kernel, stage=0, n_borrowed=None):
             cells += nC * q
         return faces + tiles + cells + nT * 9 * 8
     if kernel.startswith("k_gradient"):
-        return nC * (q + 4 + 8 + 8 * s) + tot * (4 + 4 + 2 * s) + nF * 2 * s
+        # state (the FP32 path reads its 16-byte FP32 copy), CSR, 1/V,
+        # gradient write, per cell-face neighbour index, weights and the
+        # outward area vector
+        qs = 16 if precision == 2 else q
+        return nC * (qs + 4 + 8 + 8 * s) + tot * (4 + 2 * s + 2 * s)
     if kernel.startswith("k_spectral_dt"):
-        return nC * (q + 4 + 8) + tot * 4 + nF * 2 * s + 8 * ((nC + 255) // 256)
+        return nC * (q + 4 + 8) + tot * 2 * s + 8 * ((nC + 255) // 256)
     return 0
 
 

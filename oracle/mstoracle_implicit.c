@@ -111,6 +111,7 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
   double *phi = NULL;
   int frozen = 0; /* 0 live limiter, 1 record this iteration, 2 frozen */
   int converged = 0;
+  double l2_win = 0.0;
   if (ip->freeze_tol > 0) {
     phi = (double *)calloc((size_t)8 * (m->n_faces > 0 ? m->n_faces : 1), 8);
     pp.phi = phi;
@@ -130,8 +131,14 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
     if (l2_hist) l2_hist[it] = l2;
     /* limiter freezing: the iteration after the case first falls below
      * freeze_tol records the limiter ratios, later ones reuse them */
-    if (frozen == 1) frozen = 2;
-    else if (phi && frozen == 0 && first > 0.0 && l2 <= ip->freeze_tol * first) frozen = 1;
+    if (frozen == 1) {
+      frozen = 2;
+    } else if (phi && frozen == 0 && it > 0 && it % 50 == 0) {
+      /* freeze once stagnating below freeze_tol: L2 fell by less than 30%
+       * over the last 50 iterations */
+      if (first > 0.0 && l2 <= ip->freeze_tol * first && l2 > 0.7 * l2_win) frozen = 1;
+      l2_win = l2;
+    }
     if (!converged && ip->tol > 0 && first > 0.0 && l2 <= ip->tol * first) converged = 1;
     if (converged) continue; /* the state that met the tolerance is kept */
     /* the CFL of this iteration from the norms of this residual */
@@ -154,10 +161,22 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
         double off[4];
         if (color[c] != col) continue;
         offdiag(m, q, dq, color, c, 0, p->mu, p->viscous, ip->omega, off, NULL);
-        for (j = 0; j < 4; ++j) {
-          const double v = dq[4 * (size_t)c + j] - off[j] / D[c];
-          dq[4 * (size_t)c + j] = v;
-          qn[4 * (size_t)c + j] = q[4 * (size_t)c + j] + v;
+        for (j = 0; j < 4; ++j) dq[4 * (size_t)c + j] = dq[4 * (size_t)c + j] - off[j] / D[c];
+        {
+          /* positivity: halve the update (at most 6 times, else drop it)
+           * until density and pressure stay above a fifth of their values */
+          const double *qc = q + 4 * (size_t)c, *dc = dq + 4 * (size_t)c;
+          const double p0 = kGm1 * (qc[3] - 0.5 * (qc[1] * qc[1] + qc[2] * qc[2]) / qc[0]);
+          double alpha = 1.0, n[4];
+          int ok = 0, h;
+          for (h = 0; h < 7 && !ok; ++h) {
+            double pn;
+            for (j = 0; j < 4; ++j) n[j] = qc[j] + alpha * dc[j];
+            pn = kGm1 * (n[3] - 0.5 * (n[1] * n[1] + n[2] * n[2]) / n[0]);
+            ok = n[0] > 0.2 * qc[0] && pn > 0.2 * p0;
+            if (!ok) alpha *= 0.5;
+          }
+          for (j = 0; j < 4; ++j) qn[4 * (size_t)c + j] = ok ? n[j] : qc[j];
         }
       }
     memcpy(q, qn, sizeof(double) * 4 * (size_t)nC);
