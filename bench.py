@@ -19,6 +19,14 @@ Arms:
   --impl reference   the CPU restatement of the same path (the oracle,
                      OpenMP over all host cores) on the same workload.
 
+The line also carries "batch": the batched steady-wedge family (the
+compression-ramp cases of mstcfd.meshgen.wedge_family: seeded Mach U[1.5,3],
+ramp angle U[5,15] deg redrawn within 1 deg of shock detachment, Re
+U[1e3,1e4], laminar, Roe + minmod) solved from
+free stream (cold start) to L2 1e-8 by the batched LU-SGS path in FP64 --
+wall time of the whole batch, iterations, cases converged; --batch-cases
+and --batch-cells set its size (0 cases: skipped).
+
 One JSON line on rank 0.  Under torchrun each rank runs an independent
 replica on its own GPU (single-mesh runs do not shard: replicas only).
 """
@@ -152,7 +160,7 @@ def _peaks():
 def _profile_traffic(kernel, n_cells):
     """DRAM bytes per launch of ``kernel`` from the committed ncu summary
     (per cell, scaled to this mesh), or None."""
-    path = os.path.join(ROOT, "profiles", "flux_update_vortex_ncu.txt")
+    path = os.path.join(ROOT, "profiles", "flux_update_gradient_vortex2M_ncu.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -247,6 +255,67 @@ def run_gpu(args, ws, rank, local, grp):
                          avg_launch_ms=round(avg_ms, 5), kernel_share=share), nC
 
 
+def _wedge_cases(n_cases, lo, hi):
+    """Seeded compression-ramp family: (mesh dict, Mach, angle, Re)."""
+    from mstcfd import meshgen as mg
+    return [(mg.wedge(p["cells"], p["angle"], seed=p["seed"]), p["mach"], p["angle"],
+             p["reynolds"]) for p in mg.wedge_family(n_cases, cells=(lo, hi))]
+
+
+def run_batch(args, ws, rank, grp):
+    """Cold-start batched LU-SGS solve of the wedge family to L2 1e-8.  With
+    N ranks the cases are split by greedy size balancing, each rank solves
+    its share on its own GPU (no exchange), and the wall time is the
+    maximum over ranks."""
+    from mstcfd import Mesh, batch
+    from mstcfd import meshgen as mg
+    gamma, cv = 1.4, 1.0 / (1.4 * 0.4)
+    fam = _wedge_cases(args.batch_cases, args.batch_cells[0], args.batch_cells[1])
+    mine = batch.partition_cases([m["n_cells"] for m, _, _, _ in fam], ws)[rank]
+    fam = [fam[i] for i in mine]
+    cases, q0 = [], []
+    for m, mach, angle, re in fam:
+        mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                                m["n_cells"])
+        mu = mach / re
+        cases.append((mesh, batch.case_params(mg.freestream(mach), mu=mu, lambda_=-2 / 3 * mu,
+                                              kappa=mu * gamma * cv / 0.72, cv=cv)))
+        q0.append(mg.freestream(mach, mesh.n_cells))
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters),
+                    flux=1, order=2, limiter=1, precision=1, viscous=1)
+    b.set_state(q0)
+    grp.barrier()
+    t0 = time.perf_counter()
+    r = b.solve()
+    wall = time.perf_counter() - t0
+    grp.barrier()
+    wall = grp.max(wall)
+    st = b.case_status()
+    info = b.info()
+    cells = int(sum(m.n_cells for m, _ in cases))
+    conv = st["conv_iter"]
+    n_conv = int(grp.sum((conv >= 0).sum()))
+    cells_all = int(grp.sum(cells))
+    out = {"metric": "batch time to L2 res 1e-8 (cold start, FP64)", "unit": "s",
+           "value": round(wall, 3), "device_s": round(r["ms"] * 1e-3, 3),
+           "cases": args.batch_cases, "cells": cells_all, "converged": n_conv,
+           "partition": "greedy size balancing over ranks, no exchange",
+           "iterations": r["iterations"],
+           "median_case_iterations": int(np.median(conv[conv >= 0])) if (conv >= 0).any() else None,
+           "Mcell_iterations_per_s": round(cells * r["iterations"] / (r["ms"] * 1e-3) / 1e6, 1),
+           "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
+           "graph_iters": info["graph_iters"],
+           "workload": (f"{len(cases)} compression ramps, {args.batch_cells[0]}-"
+                        f"{args.batch_cells[1]} triangles each, Mach U[1.5,3], angle U[5,15] deg "
+                        f"(attached shocks), "
+                        f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, cap "
+                        f"{args.batch_iters} iterations"),
+           "warm": None,
+           "warm_note": "learned warm start not built: no warm-start number"}
+    b.close()
+    return out
+
+
 def run_cpu_sample(m, steps, budget_s=30.0):
     """The oracle port (OpenMP over all host cores) on the workload."""
     from mstcfd import meshgen as mg
@@ -278,6 +347,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU-baseline sample (profiler runs)")
+    ap.add_argument("--batch-cases", type=int, default=16,
+                    help="cases of the batched wedge solve (0: skip)")
+    ap.add_argument("--batch-cells", type=int, nargs=2, default=[20000, 60000])
+    ap.add_argument("--batch-iters", type=int, default=8000)
     args = ap.parse_args()
     ws, rank, local = _dist()
     workload = (f"isentropic vortex, periodic jittered Delaunay {args.n}x{args.n} "
@@ -312,6 +385,7 @@ def main():
         return
     grp = _Group(ws)
     results, roof, nC = run_gpu(args, ws, rank, local, grp)
+    batch_line = run_batch(args, ws, rank, grp) if args.batch_cases > 0 else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         m = _workload(args.n)
@@ -332,7 +406,8 @@ def main():
             "e2e": {k: (round(v, 2) if isinstance(v, float) else v)
                     for k, v in results["e2e"].items()},
             "gpu_launches": fp32["launches"],
-            "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks")}
+            "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks"),
+            "batch": batch_line}
     print(json.dumps(line))
 
 

@@ -102,3 +102,18 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def partition_cases(sizes, n_parts):
+    """Greedy size balancing of independent cases over n_parts GPUs: cases
+    in decreasing size, each to the currently lightest part (ties: the
+    lowest part index).  Returns one sorted list of case indices per part.
+    Cases never interact, so the parts need no exchange."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    load = np.zeros(int(n_parts), dtype=np.int64)
+    parts = [[] for _ in range(int(n_parts))]
+    for i in sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k)):
+        p = int(np.argmin(load))
+        parts[p].append(i)
+        load[p] += sizes[i]
+    return [sorted(p) for p in parts]

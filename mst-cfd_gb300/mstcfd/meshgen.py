@@ -206,6 +206,34 @@ def wedge(cells=20000, angle_deg=10.0, seed=1, length=3.0, height=1.5, ramp_x=0.
     return _assemble(pts, tri, en, c0, c1, groups)
 
 
+def max_deflection(mach, gamma=GAMMA):
+    """Largest ramp angle (degrees) with an attached oblique shock at this
+    Mach number (the maximum of the theta-beta-Mach relation)."""
+    b = np.linspace(np.arcsin(1.0 / mach) + 1e-9, np.pi / 2, 20001)
+    t = np.arctan(2.0 / np.tan(b) * (mach ** 2 * np.sin(b) ** 2 - 1.0)
+                  / (mach ** 2 * (gamma + np.cos(2 * b)) + 2.0))
+    return float(np.degrees(t.max()))
+
+
+def wedge_family(n_cases, cells=(20000, 400000), mach=(1.5, 3.0), angle=(5.0, 15.0),
+                 reynolds=(1e3, 1e4), seed=20261204, margin_deg=1.0):
+    """Seeded parameters of the compression-ramp family: per case (Mach,
+    angle, Re, cells, mesh seed).  An angle within margin_deg of the
+    detachment angle is drawn again: with the supersonic inflow fixed at the
+    left boundary, a detached bow shock in this channel does not settle."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_cases):
+        m = rng.uniform(*mach)
+        lim = max_deflection(m) - margin_deg
+        a = rng.uniform(*angle)
+        while a >= lim:
+            a = rng.uniform(angle[0], min(angle[1], lim))
+        out.append(dict(mach=m, angle=a, reynolds=rng.uniform(*reynolds),
+                        cells=int(rng.uniform(*cells)), seed=seed + 1 + k))
+    return out
+
+
 def freestream(mach, n=None, angle_deg=0.0):
     """Free-stream conserved state, rho = 1, p = 1/gamma (speed of sound 1),
     velocity mach along angle_deg; one row, or n rows."""
