@@ -274,7 +274,7 @@ typedef struct mst_implicit_params {
   int reserved[5];
 } mst_implicit_params;
 
-/* cfl0 50, cfl_max 1000, omega 1.2, tol 1e-8, freeze_tol 1e-2,
+/* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,
  * max_iter 20000, graph_iters 20, autotune on. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
@@ -312,6 +312,55 @@ mst_status mst_batch_solve(mst_batch *b, mst_batch_result *res);
  * and the latest L2 (each nullable). */
 mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
                                  double *first_l2, double *last_l2);
+
+/* ------------------------------------------------------------------ */
+/* tensor-core GEMM of the learned initial field                       */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference.  Check entry point of the BF16
+ * tensor-core GEMM (tcgen05, accumulator in tensor memory) used by the
+ * network's dense layers: C[M][N] = A[M][K] . B[N][K]^T (+ bias[N]) (ReLU),
+ * A and B BF16 bit patterns (row-major), C FP32 (row-major), K a multiple
+ * of 64.  Host buffers; copies in and out.  layout 0 is the production
+ * descriptor layout; 1 swaps its two strides (a check of the layout). */
+mst_status mst_tc_gemm_check(const uint16_t *A, const uint16_t *B,
+                             const float *bias, float *C, int M, int N, int K,
+                             int relu, int layout);
+
+/* ------------------------------------------------------------------ */
+/* learned initial field                                                */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference.  A message-passing network over the
+ * cell adjacency predicts a steady field from cell geometry and the flow
+ * parameters, to start the batched implicit solves from:
+ *   h0 = relu(We x + be),  x = 16 features per cell
+ *   h_{l+1} = h_l + relu(Wl [h_l, mean of the neighbours' h_l] + bl),
+ *             l = 0, 1, 2, width 128
+ *   y = Wd h3 + bd,  4 outputs per cell
+ * Dense layers run on the tensor cores (BF16 operands, FP32 accumulation,
+ * both forward and backward); master weights and Adam moments FP32.
+ * Parameters, in order: We [128][64] (columns >= 16 unused), be [128],
+ * then per layer Wl [128][256], bl [128], then Wd [4][128], bd [4];
+ * row-major [outputs][inputs]. */
+typedef struct mst_mpnn mst_mpnn;
+int mst_mpnn_num_params(void);
+/* Glorot-uniform weights from a seeded generator, zero biases. */
+mst_status mst_mpnn_create(uint64_t seed, mst_mpnn **out);
+mst_status mst_mpnn_destroy(mst_mpnn *m);
+/* The graph the next forward/backward run on: features [n][16], CSR
+ * neighbour lists (nbr_ptr [n+1], nbr ids in [0, n)). */
+mst_status mst_mpnn_set_graph(mst_mpnn *m, int n, const float *features,
+                              const int *nbr_ptr, const int *nbr);
+/* Targets [n][4] of the mean-squared-error loss. */
+mst_status mst_mpnn_set_targets(mst_mpnn *m, const float *t);
+/* Outputs [n][4] (y nullable). */
+mst_status mst_mpnn_forward(mst_mpnn *m, float *y);
+/* Gradients of the loss of the last forward; loss nullable. */
+mst_status mst_mpnn_backward(mst_mpnn *m, double *loss);
+/* which = 0: parameters, 1: gradients; out [mst_mpnn_num_params()]. */
+mst_status mst_mpnn_get(mst_mpnn *m, int which, float *out);
+mst_status mst_mpnn_set_weights(mst_mpnn *m, const float *w);
+/* One Adam step (beta 0.9 / 0.999) with the current gradients. */
+mst_status mst_mpnn_adam_step(mst_mpnn *m, float lr);
 
 /* ------------------------------------------------------------------ */
 /* result writer and checkpoint files                                  */

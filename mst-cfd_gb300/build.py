@@ -12,6 +12,7 @@ Translation units are compiled in parallel for sm_103a only:
                            checkpoint files, --fmad=false
   * csrc/batch.cu          batched steady solves (LU-SGS orchestration,
                            CUDA graph, sweep autotuning)
+  * csrc/mpnn.cu           the learned initial field (tcgen05 BF16 GEMMs)
 """
 import os
 import shutil
@@ -55,6 +56,7 @@ def _units():
         ("lusgs.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "lusgs.cu")]),
         ("io.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "io.cu")]),
         ("batch.o", [nv] + common + ["-c", os.path.join(CSRC, "batch.cu")]),
+        ("mpnn.o", [nv] + common + ["-c", os.path.join(CSRC, "mpnn.cu")]),
     ]
 
 

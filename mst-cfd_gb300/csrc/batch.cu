@@ -306,7 +306,7 @@ void mst_implicit_params_default(mst_implicit_params* p) {
   if (!p) return;
   std::memset(p, 0, sizeof *p);
   p->cfl0 = 50.0;
-  p->cfl_max = 1000.0;
+  p->cfl_max = 100.0;
   p->omega = 1.2;
   p->tol = 1e-8;
   p->freeze_tol = 1e-2;

@@ -1,0 +1,623 @@
+// The learned initial field: a message-passing network over the cell
+// adjacency whose dense layers run on the tensor cores (tc_gemm.cuh).
+// This file holds the GEMM launcher and its C-ABI check entry point.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+#include "tc_gemm.cuh"
+
+namespace mst {
+namespace tc {
+
+// Descriptor strides of the no-swizzle K-major layout of k_gemm_bf16's
+// tiles: core matrices adjacent along K are 128 bytes apart (leading
+// dimension), 8-row groups 1024 bytes apart (stride dimension).
+constexpr uint32_t kLBO = 128, kSBO = 1024;
+
+cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  GemmArgs a = a0;
+  if (a.lbo == 0) {
+    a.lbo = kLBO;
+    a.sbo = kSBO;
+  }
+  dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN);
+  k_gemm_bf16<<<grid, 128, kSmemBytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace tc
+}  // namespace mst
+
+// ---------------------------------------------------------------------------
+// The network.  Per cell c of a mesh graph (interior-face neighbours N(c)):
+//   h0 = relu(We x + be)                                 x: 16 features (K 64)
+//   h_{l+1} = h_l + relu(Wl [h_l, mean_{j in N(c)} h_j] + bl),  l = 0..2
+//   y = Wd h3 + bd                                       4 outputs
+// Width 128.  GEMM operands are BF16 (weights and activations rounded once
+// per use), accumulation and the residual stream FP32; master weights and
+// Adam moments FP32.  Training minimises the mean squared error of y.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kW = 128;       // hidden width
+constexpr int kIn = 16;       // input features
+constexpr int kInK = 64;      // padded K of the first layer
+constexpr int kOut = 4;
+constexpr int kLayers = 3;
+constexpr int kZ = 2 * kW;    // [h, mean of neighbours]
+
+__global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// Z = [bf16(h_c), bf16(mean_{j in N(c)} h_j)] (rows >= n: zero)
+__global__ void k_build_z(const float* __restrict__ h, const int* __restrict__ ptr,
+                          const int* __restrict__ nbr, int n, int n_pad,
+                          __nv_bfloat16* __restrict__ z) {
+  const int c = blockIdx.x, k = threadIdx.x;  // kW threads
+  float a = 0.f, hc = 0.f;
+  if (c < n) {
+    hc = h[(size_t)c * kW + k];
+    const int b = ptr[c], e = ptr[c + 1];
+    for (int i = b; i < e; ++i) a += h[(size_t)nbr[i] * kW + k];
+    if (e > b) a /= (float)(e - b);
+  }
+  z[(size_t)c * kZ + k] = __float2bfloat16_rn(hc);
+  z[(size_t)c * kZ + kW + k] = __float2bfloat16_rn(a);
+}
+
+// dst[w][n_pad] = transpose of src[n][w] (BF16), zero for rows >= n
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ src, int n, int w,
+                                 int n_pad, __nv_bfloat16* __restrict__ dst) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    t[i][threadIdx.x] = (r < n && c < w) ? src[(size_t)r * w + c] : __float2bfloat16_rn(0.f);
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (c < w && r < n_pad) dst[(size_t)c * n_pad + r] = t[threadIdx.x][i];
+  }
+}
+
+// loss and dY = 2 (y - t) / (n * kOut); per-block partial losses
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, int n,
+                      float* __restrict__ dy, double* __restrict__ part) {
+  __shared__ double red[256];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double l = 0.0;
+  if (i < n * kOut) {
+    const float d = y[i] - t[i];
+    dy[i] = 2.f * d / (float)(n * kOut);
+    l = (double)d * d;
+  }
+  red[threadIdx.x] = l;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// dP = dH (.) [r > 0] with r = h_next - h_prev (the relu output), FP32 and a
+// BF16 copy; pad rows zero
+__global__ void k_relu_back(const float* __restrict__ dh, const float* __restrict__ hn,
+                            const float* __restrict__ hp, int n, int n_pad,
+                            float* __restrict__ dp, __nv_bfloat16* __restrict__ dpb) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n_pad * kW) return;
+  float v = 0.f;
+  if (i < (size_t)n * kW) {
+    const float r = hp ? hn[i] - hp[i] : hn[i];
+    v = r > 0.f ? dh[i] : 0.f;
+  }
+  dp[i] = v;
+  dpb[i] = __float2bfloat16_rn(v);
+}
+
+// dH_l = dH_{l+1} + dZ[:, :kW] + sum_{c in N(j)} dZ[c, kW:] / |N(c)|
+__global__ void k_agg_back(const float* __restrict__ dhn, const float* __restrict__ dz,
+                           const int* __restrict__ ptr, const int* __restrict__ nbr, int n,
+                           float* __restrict__ dh) {
+  const int j = blockIdx.x, k = threadIdx.x;
+  if (j >= n) return;
+  float v = dhn[(size_t)j * kW + k] + dz[(size_t)j * kZ + k];
+  for (int i = ptr[j]; i < ptr[j + 1]; ++i) {
+    const int c = nbr[i];
+    const int deg = ptr[c + 1] - ptr[c];
+    v += dz[(size_t)c * kZ + kW + k] / (float)deg;
+  }
+  dh[(size_t)j * kW + k] = v;
+}
+
+// column sums of g[n][w] into out[w] (bias gradients), fixed order
+__global__ void k_colsum(const float* __restrict__ g, int n, int w, float* __restrict__ out) {
+  __shared__ float red[256];
+  const int col = blockIdx.x;
+  float s = 0.f;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) s += g[(size_t)r * w + col];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[col] = red[0];
+}
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float c1,
+                       float c2, __nv_bfloat16* __restrict__ wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float x = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+  w[i] = x;
+  if (wb) wb[i] = __float2bfloat16_rn(x);
+}
+
+}  // namespace
+
+// One parameter tensor: FP32 master, BF16 copy (GEMM operand), gradient,
+// Adam moments.  Weights are [rows = outputs][cols = inputs], the B
+// operand layout of the GEMM.
+struct MpnnParam {
+  int rows = 0, cols = 0;
+  float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  __nv_bfloat16* wb = nullptr;
+  int size() const { return rows * cols; }
+};
+
+struct mst_mpnn {
+  MpnnParam W[2 * (kLayers + 2)];  // We, be, Wl0, bl0, ..., Wd, bd
+  int step = 0;
+  // work buffers for up to cap cells
+  int cap = 0;
+  int* err = nullptr;
+  double* part = nullptr;
+  std::vector<void*> bufs;
+  float* H[kLayers + 1] = {};      // FP32 residual stream
+  __nv_bfloat16 *X = nullptr, *Z[kLayers] = {}, *Hb = nullptr;
+  float *Y = nullptr, *T = nullptr, *dY = nullptr, *dH = nullptr, *dHn = nullptr,
+        *dP = nullptr, *dZ = nullptr;
+  __nv_bfloat16 *dPb = nullptr, *tA = nullptr, *tB = nullptr, *dYb = nullptr, *WdT = nullptr,
+                *WlT = nullptr;
+  int *ptr = nullptr, *nbr = nullptr;
+  int n_nbr_cap = 0;
+  int n = 0;  // cells of the current graph
+};
+
+namespace {
+
+MpnnParam& P(mst_mpnn* m, int i) { return m->W[i]; }
+enum { kWe = 0, kBe = 1, kWd = 2 * kLayers + 2, kBd = 2 * kLayers + 3 };
+int wl(int l) { return 2 + 2 * l; }
+int bl(int l) { return 3 + 2 * l; }
+
+template <class T>
+cudaError_t nalloc(mst_mpnn* m, T** p, size_t count) {
+  cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e == cudaSuccess) {
+    m->bufs.push_back(*p);
+    e = cudaMemset(*p, 0, std::max<size_t>(count, 1) * sizeof(T));
+  }
+  return e;
+}
+
+int pad128(int n) { return (n + 127) / 128 * 128; }
+int pad64(int n) { return (n + 63) / 64 * 64; }
+
+cudaError_t ensure_cap(mst_mpnn* m, int n, int n_nbr) {
+  cudaError_t e = cudaSuccess;
+  if (n_nbr > m->n_nbr_cap) {
+    if (m->nbr) cudaFree(m->nbr);
+    e = cudaMalloc(&m->nbr, sizeof(int) * (size_t)n_nbr);
+    m->n_nbr_cap = n_nbr;
+  }
+  if (e != cudaSuccess || n <= m->cap) return e;
+  // grow: free the old work buffers (parameters live in m->W)
+  for (void* p : m->bufs) cudaFree(p);
+  m->bufs.clear();
+  const int np = pad128(n), nk = pad64(n);
+  m->cap = n;
+  for (int l = 0; l <= kLayers && e == cudaSuccess; ++l) e = nalloc(m, &m->H[l], (size_t)np * kW);
+  for (int l = 0; l < kLayers && e == cudaSuccess; ++l) e = nalloc(m, &m->Z[l], (size_t)np * kZ);
+  if (e == cudaSuccess) e = nalloc(m, &m->X, (size_t)np * kInK);
+  if (e == cudaSuccess) e = nalloc(m, &m->Hb, (size_t)np * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->Y, (size_t)np * kOut);
+  if (e == cudaSuccess) e = nalloc(m, &m->T, (size_t)np * kOut);
+  if (e == cudaSuccess) e = nalloc(m, &m->dY, (size_t)np * kOut);
+  if (e == cudaSuccess) e = nalloc(m, &m->dYb, (size_t)np * kInK);
+  if (e == cudaSuccess) e = nalloc(m, &m->dH, (size_t)np * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->dHn, (size_t)np * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->dP, (size_t)np * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->dPb, (size_t)np * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->dZ, (size_t)np * kZ);
+  if (e == cudaSuccess) e = nalloc(m, &m->tA, (size_t)kZ * nk);
+  if (e == cudaSuccess) e = nalloc(m, &m->tB, (size_t)kZ * nk);
+  if (e == cudaSuccess) e = nalloc(m, &m->ptr, (size_t)n + 1);
+  if (e == cudaSuccess) e = nalloc(m, &m->part, (size_t)(np * kOut + 255) / 256 + 1);
+  if (e == cudaSuccess) e = nalloc(m, &m->err, 1);
+  if (e == cudaSuccess) e = nalloc(m, &m->WdT, (size_t)kW * kInK);
+  if (e == cudaSuccess) e = nalloc(m, &m->WlT, (size_t)kZ * kW);
+  return e;
+}
+
+cudaError_t gemm(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, float* C, int M,
+                 int N, int K, int ldc, const float* bias, int relu, int acc) {
+  mst::tc::GemmArgs g{};
+  g.A = A;
+  g.B = B;
+  g.C = C;
+  g.bias = bias;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.ldc = ldc;
+  g.relu = relu;
+  g.accumulate_c = acc;
+  g.err = m->err;
+  return mst::tc::gemm(g, 0);
+}
+
+cudaError_t transpose(const __nv_bfloat16* src, int n, int w, int n_pad, __nv_bfloat16* dst) {
+  dim3 grid((n_pad + 31) / 32, (w + 31) / 32), block(32, 8);
+  k_transpose_bf16<<<grid, block>>>(src, n, w, n_pad, dst);
+  return cudaGetLastError();
+}
+
+// forward over the graph loaded in m (n cells); Y = outputs
+cudaError_t forward(mst_mpnn* m, int n) {
+  const int np = pad128(n);
+  cudaError_t e = gemm(m, m->X, P(m, kWe).wb, m->H[0], np, kW, kInK, kW, P(m, kBe).w, 1, 0);
+  for (int l = 0; l < kLayers && e == cudaSuccess; ++l) {
+    k_build_z<<<np, kW>>>(m->H[l], m->ptr, m->nbr, n, np, m->Z[l]);
+    e = cudaMemcpyAsync(m->H[l + 1], m->H[l], sizeof(float) * (size_t)np * kW,
+                        cudaMemcpyDeviceToDevice, 0);
+    if (e == cudaSuccess)
+      e = gemm(m, m->Z[l], P(m, wl(l)).wb, m->H[l + 1], np, kW, kZ, kW, P(m, bl(l)).w, 1, 1);
+  }
+  if (e == cudaSuccess) {
+    const size_t cnt = (size_t)np * kW;
+    k_to_bf16<<<(unsigned)((cnt + 255) / 256), 256>>>(m->H[kLayers], m->Hb, cnt);
+    e = gemm(m, m->Hb, P(m, kWd).wb, m->Y, np, kOut, kW, kOut, P(m, kBd).w, 0, 0);
+  }
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+// backward of the mean squared error against m->T; gradients into W[].g;
+// returns the loss through *loss
+cudaError_t backward(mst_mpnn* m, int n, double* loss) {
+  const int np = pad128(n), nk = pad64(n);
+  const int nb = (n * kOut + 255) / 256;
+  k_mse<<<nb, 256>>>(m->Y, m->T, n, m->dY, m->part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  std::vector<double> part(nb);
+  e = cudaMemcpy(part.data(), m->part, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+  double l = 0.0;
+  for (double x : part) l += x;
+  *loss = l / (double)(n * kOut);
+  // decoder: dWd = dY^T H3, dbd = colsum dY, dH3 = dY Wd.  dY as BF16:
+  // compact [n][4] (in dPb) for the transpose, and widened to a [np][64]
+  // A operand (columns >= 4 zero) for dH3
+  e = cudaMemset(m->dYb, 0, sizeof(__nv_bfloat16) * (size_t)np * kInK);
+  if (e != cudaSuccess) return e;
+  {
+    const size_t cnt = (size_t)n * kOut;
+    k_to_bf16<<<(unsigned)((cnt + 255) / 256), 256>>>(m->dY, m->dPb, cnt);
+    e = cudaMemcpy2DAsync(m->dYb, kInK * sizeof(__nv_bfloat16), m->dPb,
+                          kOut * sizeof(__nv_bfloat16), kOut * sizeof(__nv_bfloat16), n,
+                          cudaMemcpyDeviceToDevice, 0);
+    if (e != cudaSuccess) return e;
+  }
+  e = transpose(m->dPb, n, kOut, nk, m->tA);  // dY^T [4][nk]
+  if (e == cudaSuccess) e = transpose(m->Hb, n, kW, nk, m->tB);  // H3^T [128][nk]
+  if (e == cudaSuccess)
+    e = gemm(m, m->tA, m->tB, P(m, kWd).g, kOut, kW, nk, kW, nullptr, 0, 0);
+  if (e != cudaSuccess) return e;
+  k_colsum<<<kOut, 256>>>(m->dY, n, kOut, P(m, kBd).g);
+  // dH3 = dY . Wd : B operand = Wd^T [128][64] (K = 4 padded with zeros)
+  e = transpose(P(m, kWd).wb, kOut, kW, kInK, m->WdT);
+  if (e == cudaSuccess) e = gemm(m, m->dYb, m->WdT, m->dH, np, kW, kInK, kW, nullptr, 0, 0);
+  for (int l = kLayers - 1; l >= 0 && e == cudaSuccess; --l) {
+    // dP = dH_{l+1} (.) relu'
+    const size_t cnt = (size_t)np * kW;
+    k_relu_back<<<(unsigned)((cnt + 255) / 256), 256>>>(m->dH, m->H[l + 1], m->H[l], n, np,
+                                                         m->dP, m->dPb);
+    e = transpose(m->dPb, n, kW, nk, m->tA);            // dP^T [128][nk]
+    if (e == cudaSuccess) e = transpose(m->Z[l], n, kZ, nk, m->tB);  // Z^T [256][nk]
+    if (e == cudaSuccess)
+      e = gemm(m, m->tA, m->tB, P(m, wl(l)).g, kW, kZ, nk, kZ, nullptr, 0, 0);
+    if (e != cudaSuccess) break;
+    k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, bl(l)).g);
+    // dZ = dP . Wl : B operand = Wl^T [256][128]
+    e = transpose(P(m, wl(l)).wb, kW, kZ, kW, m->WlT);
+    if (e == cudaSuccess) e = gemm(m, m->dPb, m->WlT, m->dZ, np, kZ, kW, kZ, nullptr, 0, 0);
+    if (e != cudaSuccess) break;
+    std::swap(m->dH, m->dHn);  // dHn = dH_{l+1}
+    k_agg_back<<<n, kW>>>(m->dHn, m->dZ, m->ptr, m->nbr, n, m->dH);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return e;
+  // encoder: dP0 = dH0 (.) [H0 > 0]; dWe = dP0^T X; dbe
+  {
+    const size_t cnt = (size_t)np * kW;
+    k_relu_back<<<(unsigned)((cnt + 255) / 256), 256>>>(m->dH, m->H[0], nullptr, n, np, m->dP,
+                                                         m->dPb);
+    e = transpose(m->dPb, n, kW, nk, m->tA);
+    if (e == cudaSuccess) e = transpose(m->X, n, kInK, nk, m->tB);
+    if (e == cudaSuccess)
+      e = gemm(m, m->tA, m->tB, P(m, kWe).g, kW, kInK, nk, kInK, nullptr, 0, 0);
+    if (e == cudaSuccess) k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, kBe).g);
+  }
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+}  // namespace
+namespace {
+
+// features [n][16] FP32 -> X [np][64] BF16 (zero padding)
+__global__ void k_features(const float* __restrict__ f, int n, int np,
+                           __nv_bfloat16* __restrict__ x) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)np * kInK) return;
+  const int r = (int)(i / kInK), c = (int)(i % kInK);
+  x[i] = __float2bfloat16_rn((r < n && c < kIn) ? f[(size_t)r * kIn + c] : 0.f);
+}
+
+// xorshift64* uniform in [-1, 1)
+double urand(uint64_t& s) {
+  s ^= s >> 12;
+  s ^= s << 25;
+  s ^= s >> 27;
+  const uint64_t r = s * 2685821657736338717ull;
+  return (double)(r >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mst_mpnn_num_params(void) {
+  return kW * kInK + kW + kLayers * (kW * kZ + kW) + kOut * kW + kOut;
+}
+
+mst_status mst_mpnn_create(uint64_t seed, mst_mpnn** out) {
+  if (!out) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  mst_mpnn* m = new mst_mpnn();
+  const int shapes[2 * (kLayers + 2)][2] = {{kW, kInK}, {1, kW}, {kW, kZ}, {1, kW}, {kW, kZ},
+                                            {1, kW},   {kW, kZ}, {1, kW}, {kOut, kW}, {1, kOut}};
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 * (kLayers + 2) && e == cudaSuccess; ++i) {
+    MpnnParam& p = m->W[i];
+    p.rows = shapes[i][0];
+    p.cols = shapes[i][1];
+    const size_t n = (size_t)p.size();
+    std::vector<float> w(n, 0.f);
+    if (p.rows > 1) {
+      // Glorot-uniform over the real fan-in (the first layer's is 16)
+      const int fan_in = (i == kWe) ? kIn : p.cols;
+      const double a = std::sqrt(6.0 / (fan_in + p.rows));
+      for (int r = 0; r < p.rows; ++r)
+        for (int c = 0; c < p.cols; ++c)
+          w[(size_t)r * p.cols + c] = (i == kWe && c >= kIn) ? 0.f : (float)(a * urand(st));
+    }
+    std::vector<__nv_bfloat16> wb(n);
+    for (size_t k = 0; k < n; ++k) wb[k] = __float2bfloat16_rn(w[k]);
+    e = cudaMalloc(&p.w, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&p.g, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&p.m, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&p.v, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&p.wb, n * 2);
+    if (e == cudaSuccess) e = cudaMemcpy(p.w, w.data(), n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p.wb, wb.data(), n * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(p.g, 0, n * 4);
+    if (e == cudaSuccess) e = cudaMemset(p.m, 0, n * 4);
+    if (e == cudaSuccess) e = cudaMemset(p.v, 0, n * 4);
+  }
+  if (e != cudaSuccess) {
+    mst_mpnn_destroy(m);
+    return mst_internal_fail(MST_ECUDA, std::string("mpnn create: ") + cudaGetErrorString(e));
+  }
+  *out = m;
+  return MST_OK;
+}
+
+mst_status mst_mpnn_destroy(mst_mpnn* m) {
+  if (!m) return MST_OK;
+  cudaDeviceSynchronize();
+  for (auto& p : m->W) {
+    cudaFree(p.w);
+    cudaFree(p.g);
+    cudaFree(p.m);
+    cudaFree(p.v);
+    cudaFree(p.wb);
+  }
+  for (void* p : m->bufs) cudaFree(p);
+  cudaFree(m->nbr);
+  delete m;
+  return MST_OK;
+}
+
+mst_status mst_mpnn_set_graph(mst_mpnn* m, int n, const float* features, const int* nbr_ptr,
+                              const int* nbr) {
+  if (!m || n <= 0 || !features || !nbr_ptr || !nbr)
+    return mst_internal_fail(MST_EINVAL, "bad graph arguments");
+  const int n_nbr = nbr_ptr[n];
+  for (int i = 0; i < n; ++i)
+    if (nbr_ptr[i + 1] < nbr_ptr[i]) return mst_internal_fail(MST_EINVAL, "nbr_ptr not ascending");
+  for (int i = 0; i < n_nbr; ++i)
+    if (nbr[i] < 0 || nbr[i] >= n) return mst_internal_fail(MST_EINVAL, "neighbour id out of range");
+  cudaError_t e = ensure_cap(m, n, std::max(n_nbr, 1));
+  float* df = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(float) * (size_t)n * kIn);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(df, features, sizeof(float) * (size_t)n * kIn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->ptr, nbr_ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n_nbr)
+    e = cudaMemcpy(m->nbr, nbr, sizeof(int) * (size_t)n_nbr, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    const int np = pad128(n);
+    const size_t cnt = (size_t)np * kInK;
+    k_features<<<(unsigned)((cnt + 255) / 256), 256>>>(df, n, np, m->X);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaFree(df);
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn graph: ") + cudaGetErrorString(e));
+  m->n = n;
+  return MST_OK;
+}
+
+mst_status mst_mpnn_set_targets(mst_mpnn* m, const float* t) {
+  if (!m || !t || m->n <= 0) return mst_internal_fail(MST_EINVAL, "no graph or NULL targets");
+  cudaError_t e = cudaMemcpy(m->T, t, sizeof(float) * (size_t)m->n * kOut, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));
+  return MST_OK;
+}
+
+mst_status mst_mpnn_forward(mst_mpnn* m, float* y) {
+  if (!m || m->n <= 0) return mst_internal_fail(MST_EINVAL, "no graph");
+  cudaError_t e = cudaMemset(m->err, 0, sizeof(int));
+  if (e == cudaSuccess) e = forward(m, m->n);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && y)
+    e = cudaMemcpy(y, m->Y, sizeof(float) * (size_t)m->n * kOut, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn forward: ") + cudaGetErrorString(e));
+  if (herr) return mst_internal_fail(MST_ETIMEOUT, "mpnn forward: a tensor-core wait timed out");
+  return MST_OK;
+}
+
+mst_status mst_mpnn_backward(mst_mpnn* m, double* loss) {
+  if (!m || m->n <= 0) return mst_internal_fail(MST_EINVAL, "no graph");
+  double l = 0.0;
+  cudaError_t e = backward(m, m->n, &l);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn backward: ") + cudaGetErrorString(e));
+  if (herr) return mst_internal_fail(MST_ETIMEOUT, "mpnn backward: a tensor-core wait timed out");
+  if (loss) *loss = l;
+  return MST_OK;
+}
+
+// all parameters (which = 0) or gradients (1), in the order We, be, W0, b0,
+// W1, b1, W2, b2, Wd, bd, each row-major [outputs][inputs]
+mst_status mst_mpnn_get(mst_mpnn* m, int which, float* out) {
+  if (!m || !out) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  size_t off = 0;
+  for (auto& p : m->W) {
+    const size_t n = (size_t)p.size();
+    cudaError_t e = cudaMemcpy(out + off, which ? p.g : p.w, n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));
+    off += n;
+  }
+  return MST_OK;
+}
+
+mst_status mst_mpnn_set_weights(mst_mpnn* m, const float* w) {
+  if (!m || !w) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  size_t off = 0;
+  for (auto& p : m->W) {
+    const size_t n = (size_t)p.size();
+    std::vector<__nv_bfloat16> wb(n);
+    for (size_t k = 0; k < n; ++k) wb[k] = __float2bfloat16_rn(w[off + k]);
+    cudaError_t e = cudaMemcpy(p.w, w + off, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p.wb, wb.data(), n * 2, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));
+    off += n;
+  }
+  return MST_OK;
+}
+
+mst_status mst_mpnn_adam_step(mst_mpnn* m, float lr) {
+  if (!m) return mst_internal_fail(MST_EINVAL, "NULL network");
+  m->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
+  for (auto& p : m->W) {
+    const int n = p.size();
+    k_adam<<<(n + 255) / 256, 256>>>(p.w, p.g, p.m, p.v, n, lr, b1, b2, c1, c2, p.wb);
+  }
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));
+  return MST_OK;
+}
+
+
+mst_status mst_tc_gemm_check(const uint16_t* A, const uint16_t* B, const float* bias, float* C,
+                             int M, int N, int K, int relu, int layout) {
+  if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || K % mst::tc::kBK != 0)
+    return mst_internal_fail(MST_EINVAL, "bad GEMM arguments (K must be a multiple of 64)");
+  __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+  float *dC = nullptr, *dbias = nullptr;
+  int* derr = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(dbias);
+    cudaFree(derr);
+  };
+  cudaError_t e = cudaMalloc(&dA, sizeof(uint16_t) * (size_t)M * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, sizeof(uint16_t) * (size_t)N * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, sizeof(float) * (size_t)M * N);
+  if (e == cudaSuccess && bias) e = cudaMalloc(&dbias, sizeof(float) * N);
+  if (e == cudaSuccess) e = cudaMalloc(&derr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, A, sizeof(uint16_t) * (size_t)M * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, B, sizeof(uint16_t) * (size_t)N * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && bias) e = cudaMemcpy(dbias, bias, sizeof(float) * N, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    mst::tc::GemmArgs g{};
+    g.A = dA;
+    g.B = dB;
+    g.C = dC;
+    g.bias = dbias;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.ldc = N;
+    g.relu = relu;
+    g.err = derr;
+    if (layout == 1) {  // the other assignment of the two strides
+      g.lbo = mst::tc::kSBO;
+      g.sbo = mst::tc::kLBO;
+    }
+    e = mst::tc::gemm(g, 0);
+  }
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(C, dC, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("gemm: ") + cudaGetErrorString(e));
+  if (herr) return mst_internal_fail(MST_ETIMEOUT, "gemm: a tensor-core wait timed out");
+  return MST_OK;
+}
+
+}  // extern "C"

@@ -161,6 +161,19 @@ def load():
         "mst_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
         "mst_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(BatchResult)]),
         "mst_batch_case_status": (C.c_int, [C.c_void_p, _ip, _dp, _dp]),
+        "mst_tc_gemm_check": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_int]),
+        "mst_mpnn_num_params": (C.c_int, []),
+        "mst_mpnn_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+        "mst_mpnn_destroy": (C.c_int, [C.c_void_p]),
+        "mst_mpnn_set_graph": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float), _ip, _ip]),
+        "mst_mpnn_set_targets": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "mst_mpnn_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "mst_mpnn_backward": (C.c_int, [C.c_void_p, _dp]),
+        "mst_mpnn_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
+        "mst_mpnn_set_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "mst_mpnn_adam_step": (C.c_int, [C.c_void_p, C.c_float]),
         "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
                                     C.POINTER(C.c_void_p)]),
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),

@@ -148,6 +148,9 @@ typedef struct om_params_ext {
    * 1 record, 2 use (times the current upwind difference) */
   double *phi;
   int phi_mode;
+  /* limited faces: a reconstructed side with non-positive density or
+   * pressure takes its cell value (the implicit iterations set this) */
+  int positivity;
 } om_params_ext;
 
 typedef struct om_norms {

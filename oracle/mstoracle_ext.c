@@ -192,6 +192,14 @@ void om_face_flux_ext(const om_mesh *m, const om_params_ext *p,
                 ph[4 + k] = du1 != 0.0 ? s1 / du1 : 0.0;
               }
             }
+            if (p->positivity) {
+              /* a side whose reconstructed density or pressure is not
+               * positive falls back to its cell value */
+              const double pl = (L[3] - 0.5 * (L[1] * L[1] + L[2] * L[2]) / L[0]) * (1.4 - 1.0);
+              const double pr = (R[3] - 0.5 * (R[1] * R[1] + R[2] * R[2]) / R[0]) * (1.4 - 1.0);
+              if (!(L[0] > 0.0) || !(pl > 0.0)) memcpy(L, q0, 32);
+              if (!(R[0] > 0.0) || !(pr > 0.0)) memcpy(R, q1, 32);
+            }
           }
         }
       } else {

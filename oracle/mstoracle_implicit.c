@@ -108,6 +108,7 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
   }
   for (c = 0; c < nC; ++c) ncol = color[c] + 1 > ncol ? color[c] + 1 : ncol;
   om_params_ext pp = *p;
+  pp.positivity = 1;
   double *phi = NULL;
   int frozen = 0; /* 0 live limiter, 1 record this iteration, 2 frozen */
   int converged = 0;

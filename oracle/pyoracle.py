@@ -44,7 +44,7 @@ class _OParamsExt(C.Structure):
                 ("dt", C.c_double), ("cfl", C.c_double),
                 ("inlet_q", C.c_double * 4), ("viscous", C.c_int), ("mu", C.c_double),
                 ("lam", C.c_double), ("kappa", C.c_double), ("cv", C.c_double),
-                ("phi", _dp), ("phi_mode", C.c_int)]
+                ("phi", _dp), ("phi_mode", C.c_int), ("positivity", C.c_int)]
 
 
 class _OLusgs(C.Structure):
