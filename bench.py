@@ -310,10 +310,98 @@ def run_batch(args, ws, rank, grp):
                         f"(attached shocks), "
                         f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, cap "
                         f"{args.batch_iters} iterations"),
-           "warm": None,
-           "warm_note": "learned warm start not built: no warm-start number"}
+           "warm": None}
+    q_cold = b.state()
+    conv_cold = conv
     b.close()
+    if args.warm_train > 0:
+        out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, grp)
+        if out["warm"].get("value"):
+            out["warm_speedup"] = round(out["value"] / out["warm"]["value"], 3)
     return out
+
+
+def run_warm(args, fam, cases, q_cold, conv_cold, grp):
+    """Learned warm start of the same batch: the network is trained on the
+    GPU (tensor-core forward/backward) on ramps of a disjoint seed range
+    that the batched solver converged from free stream, then predicts the
+    initial fields; the batch is solved again from them to the same
+    tolerance and the final fields are compared with the cold start's."""
+    from mstcfd import Mesh, batch, warmstart as ws
+    from mstcfd import meshgen as mg
+    from mstcfd.mpnn import Network
+    t0 = time.perf_counter()
+    train = []
+    for p in mg.wedge_family(args.warm_train, cells=(4000, 12000), seed=777):
+        m, cp = ws.case_setup(p)
+        mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                                m["n_cells"])
+        train.append((p, m, mesh, cp))
+    tb = batch.Batch([(mesh, cp) for _, _, mesh, cp in train],
+                     implicit=dict(max_iter=args.batch_iters),
+                     flux=1, order=2, limiter=1, precision=1, viscous=1)
+    tb.set_state([mg.freestream(p["mach"], mesh.n_cells) for p, _, mesh, _ in train])
+    tb.solve()
+    tconv = tb.case_status()["conv_iter"]
+    tq = tb.state()
+    tb.close()
+    samples = []
+    for k, (p, m, mesh, _) in enumerate(train):
+        if tconv[k] >= 0:
+            ptr, nbr = ws.neighbours(m)
+            samples.append((ws.features(m, mesh.arrays(), p), ptr, nbr,
+                            ws.targets(tq[k], p["mach"])))
+    data_s = time.perf_counter() - t0
+    net = Network(seed=11)
+    t1 = time.perf_counter()
+    hist = ws.train(net, samples, steps=args.warm_steps, lr=2e-3, per_step=4)
+    train_s = time.perf_counter() - t1
+    # inference for the batch's cases
+    feats = []
+    for (m, mach, angle, re), (mesh, _) in zip(fam, cases):
+        p = dict(mach=mach, angle=angle, reynolds=re)
+        ptr, nbr = ws.neighbours(m)
+        feats.append((ws.features(m, mesh.arrays(), p), ptr, nbr, mach))
+    grp.barrier()
+    t2 = time.perf_counter()
+    q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
+    infer_s = time.perf_counter() - t2
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters),
+                    flux=1, order=2, limiter=1, precision=1, viscous=1)
+    b.set_state(q_warm)
+    t3 = time.perf_counter()
+    r = b.solve()
+    solve_s = time.perf_counter() - t3
+    grp.barrier()
+    wall = grp.max(infer_s + solve_s)
+    conv = b.case_status()["conv_iter"]
+    qw = b.state()
+    b.close()
+    net.close()
+    both = [k for k in range(len(cases)) if conv[k] >= 0 and conv_cold[k] >= 0]
+    diff = max((float(np.abs(qw[k] - q_cold[k]).max() / np.abs(q_cold[k]).max()) for k in both),
+               default=None)
+    rms = max((float(np.sqrt(np.mean((qw[k] - q_cold[k]) ** 2)) / np.sqrt(np.mean(q_cold[k] ** 2)))
+               for k in both), default=None)
+    it_w = [int(conv[k]) for k in both]
+    it_c = [int(conv_cold[k]) for k in both]
+    return {"value": round(wall, 3), "unit": "s", "inference_s": round(infer_s, 3),
+            "converged": int(grp.sum((conv >= 0).sum())), "iterations": r["iterations"],
+            "median_case_iterations": int(np.median(conv[conv >= 0])) if (conv >= 0).any() else None,
+            "median_case_iterations_cold": int(np.median(conv_cold[conv_cold >= 0]))
+            if (conv_cold >= 0).any() else None,
+            "cases_converged_both": len(both),
+            "median_iterations_both": {"cold": int(np.median(it_c)) if it_c else None,
+                                       "warm": int(np.median(it_w)) if it_w else None},
+            "iteration_ratio_cold_over_warm": round(float(np.sum(it_c)) / max(np.sum(it_w), 1), 3)
+            if it_c else None,
+            "max_rel_field_diff_vs_cold": diff, "max_rms_rel_field_diff_vs_cold": rms,
+            "case_iterations": {"cold": [int(x) for x in conv_cold], "warm": [int(x) for x in conv]},
+            "train": {"cases": args.warm_train, "converged": len(samples), "cells": "4000-12000",
+                      "seeds": "disjoint from the batch", "steps": args.warm_steps,
+                      "loss_first": round(float(hist[0]), 5),
+                      "loss_last": round(float(hist[-20:].mean()), 5),
+                      "data_s": round(data_s, 2), "train_s": round(train_s, 2)}}
 
 
 def run_cpu_sample(m, steps, budget_s=30.0):
@@ -351,6 +439,9 @@ def main():
                     help="cases of the batched wedge solve (0: skip)")
     ap.add_argument("--batch-cells", type=int, nargs=2, default=[20000, 60000])
     ap.add_argument("--batch-iters", type=int, default=8000)
+    ap.add_argument("--warm-train", type=int, default=32,
+                    help="training cases of the learned warm start (0: no warm start)")
+    ap.add_argument("--warm-steps", type=int, default=400)
     args = ap.parse_args()
     ws, rank, local = _dist()
     workload = (f"isentropic vortex, periodic jittered Delaunay {args.n}x{args.n} "
