@@ -268,6 +268,13 @@ typedef struct mst_implicit_params {
    * dropped) until density and pressure stay above a fifth of their
    * current values. */
   double freeze_tol;
+  /* mixed precision (FP64 production path only): a solve starts with the
+   * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
+   * state) and switches to the FP64 residual once every unconverged case
+   * is below fp32_until * L2_first (or, with at least half of them below,
+   * when no further case has crossed it for 1000 iterations); 0: FP64
+   * residual throughout */
+  double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
   int autotune;     /* time the sweep block sizes once and keep the fastest */
@@ -275,7 +282,7 @@ typedef struct mst_implicit_params {
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,
- * max_iter 20000, graph_iters 20, autotune on. */
+ * fp32_until 0, max_iter 20000, graph_iters 20, autotune on. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {

@@ -79,9 +79,15 @@ struct mst_batch {
   double4_32a* dq = nullptr;
   double* diag = nullptr;
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
-  cudaGraphExec_t graph = nullptr;
-  int graph_iters = 0;
-  int graph_cur = 0;             // the buffer the captured iterations start from
+  // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
+  // lo is set, FP64 afterwards; the sweeps are FP64 throughout
+  bool lo = false;
+  void* grad32 = nullptr;
+  int lo_below = 0, lo_since = 0;  // phase-switch bookkeeping
+  bool tuned = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [FP64 phase, FP32 phase]
+  int graph_iters[2] = {0, 0};
+  int graph_cur[2] = {0, 0};     // the buffer the captured iterations start from
   std::vector<void*> allocs;
 };
 
@@ -103,8 +109,9 @@ mst_status bupload(mst_batch* b, T** p, const std::vector<T>& v) {
 }
 
 double4_32a* qbuf(mst_batch* b, int which) { return which ? b->ctx->q_new : b->ctx->q_old; }
+// FP32 copy of the state, kept where an FP32 residual reads it
 float4* qfbuf(mst_batch* b, int which) {
-  if (b->ctx->p.precision != MST_PREC_FP32) return nullptr;
+  if (b->ctx->p.precision != MST_PREC_FP32 && !b->lo) return nullptr;
   return which ? b->ctx->qf_new : b->ctx->qf_old;
 }
 
@@ -113,36 +120,38 @@ bool exact(const mst_batch* b) { return b->ctx->p.precision == MST_PREC_FP64_EXA
 // the residual R(Q) of the current state into ctx->r
 mst_status enqueue_residual(mst_batch* b, int which) {
   mst_ctx* c = b->ctx;
-  const int prec = c->p.precision;
+  const int prec = b->lo ? MST_PREC_FP32 : c->p.precision;
+  void* grad = b->lo ? b->grad32 : c->grad;
   cudaStream_t s = c->stream;
   const double4_32a* q = qbuf(b, which);
   const float4* qf = qfbuf(b, which);
   cudaError_t e = cudaSuccess;
   if (c->p.order == 2) {
-    if (exact(b)) e = mst::exact::launch_gradient(prec, c->dm, q, c->grad, 0, s);
+    if (exact(b) && !b->lo) e = mst::exact::launch_gradient(prec, c->dm, q, grad, 0, s);
     else if (qf)
-      e = mst::fast::launch_gradient_dt(prec, c->dm, q, qf, c->grad, 0, 0.0, nullptr, nullptr,
+      e = mst::fast::launch_gradient_dt(prec, c->dm, q, qf, grad, 0, 0.0, nullptr, nullptr,
                                         nullptr, s);
-    else e = mst::fast::launch_gradient(prec, c->dm, q, c->grad, 0, s);
+    else e = mst::fast::launch_gradient(prec, c->dm, q, grad, 0, s);
     if (e != cudaSuccess)
       return mst_internal_fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
   }
   mst::StepArgs a{};
   a.q = q;
   a.qf = qf;
-  a.grad = c->grad;
+  a.grad = grad;
   a.r_out = c->r;
   a.quirks = 0;
   a.limiter = c->p.limiter;
   mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa, c->p.cv);
   a.case_tab = b->case_tab;
   a.case_tab_f = b->case_tab_f;
-  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE) {
+  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE && !b->lo) {
     a.case_frozen = b->frozen;
     a.phi = b->phi;
   }
-  e = exact(b) ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
-               : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
+  e = (exact(b) && !b->lo)
+          ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
+          : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
   if (e != cudaSuccess)
     return mst_internal_fail(MST_ECUDA, std::string("residual: ") + cudaGetErrorString(e));
   return MST_OK;
@@ -204,7 +213,8 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.conv_iter = b->conv_iter;
   na.n_conv = b->n_conv;
   na.iter = b->iter;
-  na.frozen = b->ip.freeze_tol > 0 ? b->frozen : nullptr;
+  // the limiter-freezing state machine runs in the FP64 phase only
+  na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
   na.l2_win = b->l2_win;
   na.freeze_tol = b->ip.freeze_tol;
   na.cfl0 = b->ip.cfl0;
@@ -254,9 +264,10 @@ mst_status autotune(mst_batch* b) {
 
 mst_status build_graph(mst_batch* b, int k) {
   mst_ctx* c = b->ctx;
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
+  const int ph = b->lo ? 1 : 0;
+  if (b->graph[ph]) {
+    cudaGraphExecDestroy(b->graph[ph]);
+    b->graph[ph] = nullptr;
   }
   cudaGraph_t g = nullptr;
   B_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -273,12 +284,12 @@ mst_status build_graph(mst_batch* b, int k) {
   }
   if (e != cudaSuccess)
     return mst_internal_fail(MST_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&b->graph, g, 0);
+  e = cudaGraphInstantiate(&b->graph[ph], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess)
     return mst_internal_fail(MST_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  b->graph_iters = k;
-  b->graph_cur = b->cur;
+  b->graph_iters[ph] = k;
+  b->graph_cur[ph] = b->cur;
   return MST_OK;
 }
 
@@ -324,11 +335,13 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
   if (p->reference_quirks)
     return mst_internal_fail(MST_EINVAL, "batches run the corrected scheme (reference_quirks = 0)");
   if (!(ip->cfl0 > 0) || !(ip->cfl_max >= ip->cfl0) || !(ip->omega >= 1.0) || !(ip->tol > 0) ||
-      !(ip->freeze_tol >= 0) ||
+      !(ip->freeze_tol >= 0) || !(ip->fp32_until >= 0) ||
+      (ip->fp32_until > 0 && p->precision == MST_PREC_FP64_EXACT) ||
       ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1))
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
-                             "tol > 0, max_iter >= 0, graph_iters >= 0 and even");
+                             "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0 "
+                             "(0 on the exact path)");
   std::unique_ptr<mst_batch> b(new mst_batch());
   b->ip = *ip;
   b->n_cases = n_cases;
@@ -418,6 +431,8 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
                        (p->precision == MST_PREC_FP32 ? sizeof(float) : sizeof(double)))) ||
       (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
+      (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
+                                            ? sizeof(float) * 8 * (size_t)nC : 0)) ||
       (st = reset_progress(b.get()))) {
     cleanup();
     return st;
@@ -433,7 +448,8 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
 mst_status mst_batch_destroy(mst_batch* b) {
   if (!b) return MST_OK;
   if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (int i = 0; i < 2; ++i)
+    if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
   for (void* p : b->allocs) cudaFree(p);
   if (b->ctx) mst_ctx_destroy(b->ctx);
   delete b->mesh;
@@ -448,7 +464,7 @@ mst_status mst_batch_info(const mst_batch* b, mst_batch_info_t* info) {
   info->n_faces = b->mesh->host.n_faces;
   info->n_colors = b->n_colors;
   info->sweep_threads = b->threads;
-  info->graph_iters = b->graph_iters;
+  info->graph_iters = std::max(b->graph_iters[0], b->graph_iters[1]);
   return MST_OK;
 }
 
@@ -463,6 +479,15 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   mst_status st = mst_set_state(b->ctx, q, 4);
   if (st) return st;
   b->cur = 0;
+  // a new solve starts in the FP32-residual phase when one is configured
+  b->lo = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
+  b->lo_below = 0;
+  b->lo_since = 0;
+  if (b->lo) {
+    cudaError_t e = mst::fast::launch_to_f32(b->ctx->q_old, b->ctx->qf_old, b->ctx->dm.n_cells,
+                                             b->ctx->stream);
+    if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));
+  }
   st = reset_progress(b);
   if (st) return st;
   B_CU(cudaStreamSynchronize(b->ctx->stream));
@@ -494,27 +519,35 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
   mst_ctx* c = b->ctx;
   mst_status st;
-  if (b->ip.autotune && b->graph_iters == 0) {
+  if (b->ip.autotune && !b->tuned) {
     st = autotune(b);
     if (st) return st;
+    b->tuned = true;
   }
   const int k = b->ip.graph_iters;
-  if (k > 0 && (b->graph_iters != k || b->graph_cur != b->cur)) {
-    // the kernels' one-time attribute setup runs before capture
-    st = enqueue_residual(b, b->cur);
-    if (st) return st;
-    B_CU(cudaStreamSynchronize(c->stream));
-    st = build_graph(b, k);
-    if (st) return st;
-  }
+  auto ensure_graph = [&]() -> mst_status {
+    const int ph = b->lo ? 1 : 0;
+    if (k > 0 && (b->graph_iters[ph] != k || b->graph_cur[ph] != b->cur || !b->graph[ph])) {
+      // the kernels' one-time attribute setup runs before capture
+      mst_status s2 = enqueue_residual(b, b->cur);
+      if (s2) return s2;
+      B_CU(cudaStreamSynchronize(c->stream));
+      return build_graph(b, k);
+    }
+    return MST_OK;
+  };
+  st = ensure_graph();
+  if (st) return st;
   int h[2] = {0, 0};
   B_CU(cudaMemcpy(&h[0], b->iter, sizeof(int), cudaMemcpyDeviceToHost));
   const int start = h[0];
   B_CU(cudaEventRecord(c->ev0, c->stream));
   int done = 0, iters = 0;
+  std::vector<double> f(b->n_cases), l(b->n_cases);
+  std::vector<int> cv(b->n_cases);
   while (iters < b->ip.max_iter) {
     if (k > 0 && iters + k <= b->ip.max_iter) {
-      B_CU(cudaGraphLaunch(b->graph, c->stream));
+      B_CU(cudaGraphLaunch(b->graph[b->lo ? 1 : 0], c->stream));
       iters += k;  // k is even: the state is back in the same buffer
     } else {
       st = run_iterations(b, 1);
@@ -525,6 +558,25 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     B_CU(cudaStreamSynchronize(c->stream));
     done = h[1];
     if (done >= b->n_cases) break;
+    if (b->lo) {
+      // leave the FP32 phase once every unconverged case is below
+      // fp32_until, or when no further case has crossed it for 1000
+      // iterations while at least half of them have
+      B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
+      B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
+      int below = 0;
+      for (int i = 0; i < b->n_cases; ++i) below += (l[i] <= b->ip.fp32_until * f[i]) ? 1 : 0;
+      if (below > b->lo_below) {
+        b->lo_below = below;
+        b->lo_since = iters;
+      }
+      if (below == b->n_cases ||
+          (2 * below >= b->n_cases && iters - b->lo_since >= 1000)) {
+        b->lo = false;
+        st = ensure_graph();
+        if (st) return st;
+      }
+    }
   }
   B_CU(cudaEventRecord(c->ev1, c->stream));
   B_CU(cudaEventSynchronize(c->ev1));

@@ -229,3 +229,26 @@ def test_gpu_batch_production_precisions_track_exact(prec):
     tol = 1e-9 if prec == 1 else 2e-4
     for a, c in zip(out[0], out[prec]):
         assert np.abs(a - c).max() <= tol * np.abs(a).max()
+
+
+@pytest.mark.gpu
+def test_gpu_batch_mixed_precision_reaches_tolerance():
+    """FP32 residual until 1e-3, then FP64: every case reaches 1e-8 and the
+    converged fields agree with the FP64-only solve."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    out = {}
+    for fp32 in (0.0, 1e-3):
+        b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                        implicit=dict(fp32_until=fp32, max_iter=4000),
+                        flux=1, order=2, limiter=1, precision=1)
+        b.set_state(q0)
+        r = b.solve()
+        assert r["n_converged"] == len(cases), fp32
+        out[fp32] = b.state()
+        b.close()
+    for a, c in zip(out[0.0], out[1e-3]):
+        rms = np.sqrt(np.mean((a - c) ** 2)) / np.sqrt(np.mean(a ** 2))
+        assert rms < 1e-3
