@@ -328,7 +328,9 @@ mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
  * network's dense layers: C[M][N] = A[M][K] . B[N][K]^T (+ bias[N]) (ReLU),
  * A and B BF16 bit patterns (row-major), C FP32 (row-major), K a multiple
  * of 64.  Host buffers; copies in and out.  layout 0 is the production
- * descriptor layout; 1 swaps its two strides (a check of the layout). */
+ * descriptor layout; 1 swaps its two strides (a check of the layout); a
+ * multiple of 64 splits K into chunks of that size over separate CTAs
+ * whose partial products are added in a fixed order (no bias / ReLU). */
 mst_status mst_tc_gemm_check(const uint16_t *A, const uint16_t *B,
                              const float *bias, float *C, int M, int N, int K,
                              int relu, int layout);

@@ -33,9 +33,20 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
     a.lbo = kLBO;
     a.sbo = kSBO;
   }
-  dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN);
+  const int splits = a.k_chunk > 0 ? (a.K + a.k_chunk - 1) / a.k_chunk : 1;
+  dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN, splits);
   k_gemm_bf16<<<grid, 128, kSmemBytes, s>>>(a);
   return cudaGetLastError();
+}
+
+// C[M][N] = sum over z of part[z][M][N], in z order (deterministic)
+__global__ void k_reduce_splits(const float* __restrict__ part, int splits, size_t mn,
+                                float* __restrict__ c) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= mn) return;
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(size_t)z * mn + i];
+  c[i] = s;
 }
 
 }  // namespace tc
@@ -58,6 +69,7 @@ constexpr int kInK = 64;      // padded K of the first layer
 constexpr int kOut = 4;
 constexpr int kLayers = 3;
 constexpr int kZ = 2 * kW;    // [h, mean of neighbours]
+constexpr int kMaxSplits = 64;  // split-K CTAs of a weight-gradient GEMM
 
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -195,7 +207,7 @@ struct mst_mpnn {
   // work buffers for up to cap cells
   int cap = 0;
   int* err = nullptr;
-  double* part = nullptr;
+  double* lpart = nullptr;
   std::vector<void*> bufs;
   float* H[kLayers + 1] = {};      // FP32 residual stream
   __nv_bfloat16 *X = nullptr, *Z[kLayers] = {}, *Hb = nullptr;
@@ -203,6 +215,7 @@ struct mst_mpnn {
         *dP = nullptr, *dZ = nullptr;
   __nv_bfloat16 *dPb = nullptr, *tA = nullptr, *tB = nullptr, *dYb = nullptr, *WdT = nullptr,
                 *WlT = nullptr;
+  float* part = nullptr;  // split-K partial products of the weight gradients
   int *ptr = nullptr, *nbr = nullptr;
   int n_nbr_cap = 0;
   int n = 0;  // cells of the current graph
@@ -257,10 +270,11 @@ cudaError_t ensure_cap(mst_mpnn* m, int n, int n_nbr) {
   if (e == cudaSuccess) e = nalloc(m, &m->tA, (size_t)kZ * nk);
   if (e == cudaSuccess) e = nalloc(m, &m->tB, (size_t)kZ * nk);
   if (e == cudaSuccess) e = nalloc(m, &m->ptr, (size_t)n + 1);
-  if (e == cudaSuccess) e = nalloc(m, &m->part, (size_t)(np * kOut + 255) / 256 + 1);
+  if (e == cudaSuccess) e = nalloc(m, &m->lpart, (size_t)(np * kOut + 255) / 256 + 1);
   if (e == cudaSuccess) e = nalloc(m, &m->err, 1);
   if (e == cudaSuccess) e = nalloc(m, &m->WdT, (size_t)kW * kInK);
   if (e == cudaSuccess) e = nalloc(m, &m->WlT, (size_t)kZ * kW);
+  if (e == cudaSuccess) e = nalloc(m, &m->part, (size_t)kMaxSplits * kW * kZ);
   return e;
 }
 
@@ -279,6 +293,32 @@ cudaError_t gemm(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, fl
   g.accumulate_c = acc;
   g.err = m->err;
   return mst::tc::gemm(g, 0);
+}
+
+// Weight gradients: M, N small (<= 256), K = the number of cells.  Split K
+// over up to kMaxSplits CTAs per output tile, then add the partial products
+// in a fixed order.
+cudaError_t gemm_wgrad(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, float* C,
+                       int M, int N, int K, int ldc) {
+  const int kt = K / mst::tc::kBK;  // K tiles
+  const int splits = std::min(kMaxSplits, std::max(1, kt / 8));
+  const int chunk = ((kt + splits - 1) / splits) * mst::tc::kBK;
+  const int used = (K + chunk - 1) / chunk;
+  mst::tc::GemmArgs g{};
+  g.A = A;
+  g.B = B;
+  g.C = m->part;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.ldc = ldc;
+  g.err = m->err;
+  g.k_chunk = chunk;
+  cudaError_t e = mst::tc::gemm(g, 0);
+  if (e != cudaSuccess) return e;
+  const size_t mn = (size_t)M * ldc;
+  mst::tc::k_reduce_splits<<<(unsigned)((mn + 255) / 256), 256>>>(m->part, used, mn, C);
+  return cudaGetLastError();
 }
 
 cudaError_t transpose(const __nv_bfloat16* src, int n, int w, int n_pad, __nv_bfloat16* dst) {
@@ -311,11 +351,11 @@ cudaError_t forward(mst_mpnn* m, int n) {
 cudaError_t backward(mst_mpnn* m, int n, double* loss) {
   const int np = pad128(n), nk = pad64(n);
   const int nb = (n * kOut + 255) / 256;
-  k_mse<<<nb, 256>>>(m->Y, m->T, n, m->dY, m->part);
+  k_mse<<<nb, 256>>>(m->Y, m->T, n, m->dY, m->lpart);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   std::vector<double> part(nb);
-  e = cudaMemcpy(part.data(), m->part, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+  e = cudaMemcpy(part.data(), m->lpart, sizeof(double) * nb, cudaMemcpyDeviceToHost);
   double l = 0.0;
   for (double x : part) l += x;
   *loss = l / (double)(n * kOut);
@@ -335,7 +375,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
   e = transpose(m->dPb, n, kOut, nk, m->tA);  // dY^T [4][nk]
   if (e == cudaSuccess) e = transpose(m->Hb, n, kW, nk, m->tB);  // H3^T [128][nk]
   if (e == cudaSuccess)
-    e = gemm(m, m->tA, m->tB, P(m, kWd).g, kOut, kW, nk, kW, nullptr, 0, 0);
+    e = gemm_wgrad(m, m->tA, m->tB, P(m, kWd).g, kOut, kW, nk, kW);
   if (e != cudaSuccess) return e;
   k_colsum<<<kOut, 256>>>(m->dY, n, kOut, P(m, kBd).g);
   // dH3 = dY . Wd : B operand = Wd^T [128][64] (K = 4 padded with zeros)
@@ -349,7 +389,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
     e = transpose(m->dPb, n, kW, nk, m->tA);            // dP^T [128][nk]
     if (e == cudaSuccess) e = transpose(m->Z[l], n, kZ, nk, m->tB);  // Z^T [256][nk]
     if (e == cudaSuccess)
-      e = gemm(m, m->tA, m->tB, P(m, wl(l)).g, kW, kZ, nk, kZ, nullptr, 0, 0);
+      e = gemm_wgrad(m, m->tA, m->tB, P(m, wl(l)).g, kW, kZ, nk, kZ);
     if (e != cudaSuccess) break;
     k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, bl(l)).g);
     // dZ = dP . Wl : B operand = Wl^T [256][128]
@@ -369,7 +409,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
     e = transpose(m->dPb, n, kW, nk, m->tA);
     if (e == cudaSuccess) e = transpose(m->X, n, kInK, nk, m->tB);
     if (e == cudaSuccess)
-      e = gemm(m, m->tA, m->tB, P(m, kWe).g, kW, kInK, nk, kInK, nullptr, 0, 0);
+      e = gemm_wgrad(m, m->tA, m->tB, P(m, kWe).g, kW, kInK, nk, kInK);
     if (e == cudaSuccess) k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, kBe).g);
   }
   return e == cudaSuccess ? cudaGetLastError() : e;
@@ -608,7 +648,24 @@ mst_status mst_tc_gemm_check(const uint16_t* A, const uint16_t* B, const float* 
       g.lbo = mst::tc::kSBO;
       g.sbo = mst::tc::kLBO;
     }
-    e = mst::tc::gemm(g, 0);
+    if (layout >= mst::tc::kBK && layout % mst::tc::kBK == 0 && !bias && !relu) {
+      // split K in chunks of `layout`, partial products reduced in order
+      const int splits = (K + layout - 1) / layout;
+      float* part = nullptr;
+      e = cudaMalloc(&part, sizeof(float) * (size_t)splits * M * N);
+      if (e == cudaSuccess) {
+        g.C = part;
+        g.k_chunk = layout;
+        e = mst::tc::gemm(g, 0);
+        const size_t mn = (size_t)M * N;
+        if (e == cudaSuccess)
+          mst::tc::k_reduce_splits<<<(unsigned)((mn + 255) / 256), 256>>>(part, splits, mn, dC);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(part);
+      }
+    } else {
+      e = mst::tc::gemm(g, 0);
+    }
   }
   int herr = 0;
   if (e == cudaSuccess) e = cudaDeviceSynchronize();

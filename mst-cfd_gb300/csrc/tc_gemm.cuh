@@ -128,6 +128,10 @@ struct GemmArgs {
   int accumulate_c;        // C += result (FP32 output only)
   uint32_t lbo, sbo;       // descriptor strides (bytes)
   int* err;                // set on a timed-out wait
+  // split K: CTA z covers K range [z * k_chunk, (z + 1) * k_chunk) and
+  // writes its partial product to C + z * M * ldc (no bias / ReLU);
+  // k_chunk = 0: one CTA per output tile over the whole K
+  int k_chunk;
 };
 
 __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
@@ -139,7 +143,11 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   volatile int* s_ok = reinterpret_cast<volatile int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
-  const int T = g.K / kBK;
+  const bool split = g.k_chunk > 0;
+  const int kbase = split ? blockIdx.z * g.k_chunk : 0;
+  const int klen = split ? min(g.k_chunk, g.K - kbase) : g.K;
+  const int T = klen / kBK;
+  float* Cout = (split && g.C) ? g.C + (size_t)blockIdx.z * g.M * g.ldc : g.C;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   const uint32_t tmem = *tslot;
 
   auto load_tile = [&](int t, int s) {
-    const int k0 = t * kBK;
+    const int k0 = kbase + t * kBK;
     const uint32_t a0 = smem_u32(sA + s * kTileA), b0 = smem_u32(sB + s * kTileB);
     // 128 rows x 8 chunks of 16 bytes for A, BN x 8 for B
     for (int c = tid; c < kBM * 8; c += 128) {
@@ -211,7 +219,8 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
     }
     ++issued;
   }
-  // wait for the last committed tile (its commit covers all earlier MMAs)
+  // wait for the last committed tile (its commit covers all earlier MMAs);
+  // the host sizes split-K chunks so that every CTA has a K tile
   if (ok && issued > 0) {
     const int tl = issued - 1;
     if (tid == 0 && !mbar_wait(&bars[tl & 1], (tl >> 1) & 1)) *s_ok = 0;
@@ -233,12 +242,12 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
         for (int i = 0; i < 16; ++i) {
           const int col = n0 + c0 + i;
           float x = v[i];
-          if (g.bias && col < g.N) x += g.bias[col];
-          if (g.relu) x = fmaxf(x, 0.f);
+          if (!split && g.bias && col < g.N) x += g.bias[col];
+          if (!split && g.relu) x = fmaxf(x, 0.f);
           if (col < g.N) {
-            if (g.C) {
-              float* p = g.C + (size_t)row * g.ldc + col;
-              *p = g.accumulate_c ? *p + x : x;
+            if (Cout) {
+              float* p = Cout + (size_t)row * g.ldc + col;
+              *p = (!split && g.accumulate_c) ? *p + x : x;
             }
             if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
           }

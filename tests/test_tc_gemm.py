@@ -54,3 +54,14 @@ def test_tc_gemm_matches_numpy(M, N, K, relu, bias):
     assert st == capi.OK, capi.load().mst_last_error()
     tol = 1e-5 * np.sqrt(K) * (np.abs(ref).max() + 1)
     assert np.abs(got - ref).max() <= tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("M,N,K,chunk", [(128, 256, 4096, 512), (4, 128, 2048, 192),
+                                         (128, 64, 1280, 64)])
+def test_tc_gemm_split_k(M, N, K, chunk):
+    from mstcfd import capi
+    st, got, ref = _run(M, N, K, 0, 0, layout=chunk, seed=2)
+    assert st == capi.OK, capi.load().mst_last_error()
+    tol = 1e-5 * np.sqrt(K) * (np.abs(ref).max() + 1)
+    assert np.abs(got - ref).max() <= tol
