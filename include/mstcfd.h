@@ -142,6 +142,37 @@ typedef struct mst_mesh_arrays {
 } mst_mesh_arrays;
 mst_status mst_mesh_get_arrays(const mst_mesh *m, mst_mesh_arrays *a);
 
+/* 3D meshes: MshBlock::readMsh with DIM 3 (mesh/MshBlock.cpp:436-789) --
+ * triangular/quadrilateral faces, zones with a fixed face node count as the
+ * reference reads them and, beyond it, mixed zones (node count 0 in the
+ * zone header, each face line led by its node count).  Geometry by the
+ * reference's 3D formulas (Face.cpp:20-39, Cell.cpp:6-14, :52-59; its cell
+ * volume is the incomplete formula of the reference) plus the corrected
+ * divergence-theorem volume.  Host only: no 3D residual kernels exist. */
+typedef struct mst_mesh3d mst_mesh3d;
+typedef struct mst_mesh3d_info {
+  int n_nodes, n_cells, n_faces, n_int_faces, n_zones, n_face_nodes, n_cell_faces,
+      n_cell_nodes, n_inner, n_bond1, n_bond2;
+} mst_mesh3d_info;
+typedef struct mst_mesh3d_arrays {
+  double *node_xyz;                                   /* [nN][3] */
+  int *face_ptr, *face_nodes, *face_cells, *face_type; /* [nF+1], [..], [nF][2], [nF] */
+  double *face_ctr, *face_dir, *face_area, *face_eta0; /* [nF][3], [nF][3], [nF], [nF] */
+  double *face_cmd;     /* [nF][3] centre minus the mean of the two cell centres */
+  int *face_dac;        /* [nF] */
+  uint8_t *face_flag, *face_flag_set;  /* [nF][3] where set, [nF] */
+  int *cell_ptr, *cell_faces, *cell_nb;               /* CSR, file order */
+  double *cell_dof, *cell_eta0c;                      /* [tot][3], [tot] */
+  double *cell_ctr, *cell_vol, *cell_vol_fixed;       /* [nC][3], [nC], [nC] */
+  int *cell_node_ptr, *cell_nodes;                    /* reader's node order */
+  int *inner, *bond1, *bond2, *cell_n_lower;
+} mst_mesh3d_arrays;
+mst_status mst_mesh3d_read_msh(const char *path, mst_mesh3d **out);
+mst_status mst_mesh3d_get_info(const mst_mesh3d *m, mst_mesh3d_info *info);
+/* Copies out the arrays; every pointer may be NULL. */
+mst_status mst_mesh3d_get_arrays(const mst_mesh3d *m, mst_mesh3d_arrays *a);
+void mst_mesh3d_destroy(mst_mesh3d *m);
+
 /* ------------------------------------------------------------------ */
 /* solver contexts: the RhoSolver surface                              */
 /* ------------------------------------------------------------------ */

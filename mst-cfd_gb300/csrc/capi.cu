@@ -517,6 +517,72 @@ mst_status mst_mesh_create(const mst_mesh_desc* d, mst_mesh** out) {
 
 void mst_mesh_destroy(mst_mesh* m) { delete m; }
 
+mst_status mst_mesh3d_read_msh(const char* path, mst_mesh3d** out) {
+  if (!path || !out) return fail(MST_EINVAL, "NULL argument");
+  *out = nullptr;
+  std::unique_ptr<mst_mesh3d> m(new mst_mesh3d());
+  std::string err;
+  int rc = mst::read_msh3d(path, &m->host, &err);
+  if (rc != mst::kOk) return fail(rc == mst::kEMesh ? MST_EMESH : MST_EINVAL, err);
+  *out = m.release();
+  return MST_OK;
+}
+
+mst_status mst_mesh3d_get_info(const mst_mesh3d* m, mst_mesh3d_info* info) {
+  if (!m || !info) return fail(MST_EINVAL, "NULL argument");
+  const auto& h = m->host;
+  info->n_nodes = h.n_nodes;
+  info->n_cells = h.n_cells;
+  info->n_faces = h.n_faces;
+  info->n_int_faces = h.n_int_faces;
+  info->n_zones = (int)h.zone.size() / 4;
+  info->n_face_nodes = (int)h.face_nodes.size();
+  info->n_cell_faces = (int)h.cell_faces.size();
+  info->n_cell_nodes = (int)h.cell_nodes.size();
+  info->n_inner = (int)h.inner.size();
+  info->n_bond1 = (int)h.bond1.size();
+  info->n_bond2 = (int)h.bond2.size();
+  return MST_OK;
+}
+
+mst_status mst_mesh3d_get_arrays(const mst_mesh3d* m, mst_mesh3d_arrays* a) {
+  if (!m || !a) return fail(MST_EINVAL, "NULL argument");
+  const auto& h = m->host;
+  auto cp = [](auto* dst, const auto& v) {
+    if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+  };
+  cp(a->node_xyz, h.node_xyz);
+  cp(a->face_ptr, h.face_ptr);
+  cp(a->face_nodes, h.face_nodes);
+  cp(a->face_cells, h.face_cells);
+  cp(a->face_type, h.face_type);
+  cp(a->face_ctr, h.face_ctr);
+  cp(a->face_dir, h.face_dir);
+  cp(a->face_area, h.face_area);
+  cp(a->face_eta0, h.face_eta0);
+  cp(a->face_cmd, h.face_cmd);
+  cp(a->face_dac, h.face_dac);
+  cp(a->face_flag, h.face_flag);
+  cp(a->face_flag_set, h.face_flag_set);
+  cp(a->cell_ptr, h.cell_ptr);
+  cp(a->cell_faces, h.cell_faces);
+  cp(a->cell_nb, h.cell_nb);
+  cp(a->cell_dof, h.cell_dof);
+  cp(a->cell_eta0c, h.cell_eta0c);
+  cp(a->cell_ctr, h.cell_ctr);
+  cp(a->cell_vol, h.cell_vol);
+  cp(a->cell_vol_fixed, h.cell_vol_fixed);
+  cp(a->cell_node_ptr, h.cell_node_ptr);
+  cp(a->cell_nodes, h.cell_nodes);
+  cp(a->inner, h.inner);
+  cp(a->bond1, h.bond1);
+  cp(a->bond2, h.bond2);
+  cp(a->cell_n_lower, h.cell_nL);
+  return MST_OK;
+}
+
+void mst_mesh3d_destroy(mst_mesh3d* m) { delete m; }
+
 mst_status mst_mesh_get_info(const mst_mesh* m, mst_mesh_info* info) {
   if (!m || !info) return fail(MST_EINVAL, "NULL argument");
   const auto& h = m->host;

@@ -18,6 +18,10 @@ struct mst_mesh {
   mst::DevLayout lay;
 };
 
+struct mst_mesh3d {
+  mst::HostMesh3D host;
+};
+
 struct DevArrays {
   int2* f_c0c1 = nullptr;
   int* f_info = nullptr;

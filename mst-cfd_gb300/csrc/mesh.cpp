@@ -672,4 +672,346 @@ int build_union(const std::vector<const HostMesh*>& parts, HostMesh* out,
   return kOk;
 }
 
+
+// ---------------------------------------------------------------------------
+// 3D reader (MshBlock::splitInformationData3D / dataToMesh3D,
+// mesh/MshBlock.cpp:436-789) and the reference's 3D geometry.
+// ---------------------------------------------------------------------------
+namespace {
+
+typedef double V3[3];
+
+inline void sub3(const double* a, const double* b, double* o) {
+  o[0] = a[0] - b[0];
+  o[1] = a[1] - b[1];
+  o[2] = a[2] - b[2];
+}
+// Eigen-style dot / norm: left-to-right sums
+inline double dot3(const double* a, const double* b) {
+  double s = a[0] * b[0];
+  s += a[1] * b[1];
+  s += a[2] * b[2];
+  return s;
+}
+inline double norm3(const double* a) { return std::sqrt(dot3(a, a)); }
+
+}  // namespace
+
+int read_msh3d(const std::string& path, HostMesh3D* m, std::string* err) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) {
+    *err = "cannot open " + path;
+    return kEInval;
+  }
+  std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  std::vector<std::string> hdr, dat;
+  dat.emplace_back();
+  size_t b = 0;
+  while (b < text.size()) {
+    size_t e = text.find('\n', b);
+    if (e == std::string::npos) e = text.size();
+    std::string line = text.substr(b, e - b);
+    while (!line.empty() && line.back() == '\r') line.pop_back();
+    if (!line.empty() && (line[0] == '(' || line[0] == ')')) hdr.push_back(line);
+    else dat.push_back(line);
+    b = e + 1;
+  }
+  int nN = -1, nC = -1, nF = -1;
+  for (const auto& s : hdr) {
+    std::string br;
+    if (s.size() < 3 || s[1] != '1' || !second_bracket(s, &br) || br.empty() || br[0] != '0')
+      continue;
+    auto t = split_spaces(br);
+    if (t.size() < 3) continue;
+    int v = hex_value(t[2]);
+    if (s[2] == '0') nN = v;
+    if (s[2] == '2') nC = v;
+    if (s[2] == '3') nF = v;
+  }
+  if (nN <= 0 || nC <= 0 || nF <= 0) {
+    *err = "missing node/cell/face totals";
+    return kEMesh;
+  }
+  HostMesh3D& M = *m;
+  M = HostMesh3D{};
+  M.n_nodes = nN;
+  M.n_cells = nC;
+  M.n_faces = nF;
+  M.node_xyz.assign(3 * (size_t)nN, 0.0);
+  M.face_ptr.assign(1, 0);
+  M.face_cells.assign(2 * (size_t)nF, -1);
+  M.face_type.assign(nF, 0);
+  size_t di = 0;
+  int flag_node = 0, flag_face = 0;
+  for (const auto& s : hdr) {
+    std::string br;
+    if (s.size() < 3 || s[1] != '1' || !second_bracket(s, &br) || br.empty() || br[0] == '0')
+      continue;
+    if (s[2] == '0') {
+      ++di;  // the first data line is skipped, as in the 2D reader
+      for (; flag_node < nN; ++flag_node) {
+        if (di >= dat.size()) {
+          *err = "node section truncated";
+          return kEMesh;
+        }
+        auto t = split_spaces(dat[di++]);
+        if (t.size() < 3) {
+          *err = "bad 3D node line";
+          return kEMesh;
+        }
+        for (int d = 0; d < 3; ++d)
+          M.node_xyz[3 * (size_t)flag_node + d] = std::strtod(t[d].c_str(), nullptr);
+      }
+    } else if (s[2] == '3') {
+      auto t = split_spaces(br);
+      if (t.size() < 5) {
+        *err = "bad face zone header";
+        return kEMesh;
+      }
+      int zid = hex_value(t[0]), st = hex_value(t[1]), en = hex_value(t[2]), ty = hex_value(t[3]),
+          nn = hex_value(t[4]);
+      if (en > nF || st != flag_face + 1 || !(nn == 0 || nn == 3 || nn == 4)) {
+        *err = "unsupported face zone (gaps or face node count other than 3, 4, mixed)";
+        return kEMesh;
+      }
+      M.zone.insert(M.zone.end(), {zid, st, en, ty});
+      if (ty == kInterior) M.n_int_faces = en;
+      for (; flag_face < en; ++flag_face) {
+        if (di >= dat.size()) {
+          *err = "face section truncated";
+          return kEMesh;
+        }
+        auto tk = split_spaces(dat[di++]);
+        size_t p0 = 0;
+        int k = nn;
+        if (nn == 0) {  // mixed zone: the line starts with its node count
+          if (tk.empty()) {
+            *err = "bad mixed face line";
+            return kEMesh;
+          }
+          k = hex_value(tk[0]);
+          p0 = 1;
+          if (k != 3 && k != 4) {
+            *err = "mixed face with a node count other than 3 or 4";
+            return kEMesh;
+          }
+        }
+        const size_t need = p0 + k + ((ty == kInterior) ? 2 : 1);
+        if (tk.size() < need) {
+          *err = "bad face line";
+          return kEMesh;
+        }
+        for (int j = 0; j < k; ++j) {
+          const int nd = hex_value(tk[p0 + j]) - 1;
+          if (nd < 0 || nd >= nN) {
+            *err = "face references a missing node";
+            return kEMesh;
+          }
+          M.face_nodes.push_back(nd);
+        }
+        M.face_ptr.push_back((int)M.face_nodes.size());
+        const int c0 = hex_value(tk[p0 + k]) - 1;
+        const int c1 = (ty == kInterior) ? hex_value(tk[p0 + k + 1]) - 1 : -1;
+        if (c0 < 0 || c0 >= nC || (ty == kInterior && (c1 < 0 || c1 >= nC))) {
+          *err = "face references a missing cell";
+          return kEMesh;
+        }
+        M.face_cells[2 * (size_t)flag_face] = c0;
+        M.face_cells[2 * (size_t)flag_face + 1] = c1;
+        M.face_type[flag_face] = ty;
+      }
+    }
+  }
+  if (flag_node != nN || flag_face != nF || M.zone.empty()) {
+    *err = "node or face sections incomplete";
+    return kEMesh;
+  }
+  // cell -> face lists in file order (c0 then c1 of each face line), and
+  // the neighbour per cell-face (the cell itself on boundary faces)
+  std::vector<std::vector<int>> cf(nC), cn(nC);
+  for (int f = 0; f < nF; ++f) {
+    const int c0 = M.face_cells[2 * f], c1 = M.face_cells[2 * f + 1];
+    cf[c0].push_back(f);
+    if (c1 >= 0) {
+      cf[c1].push_back(f);
+      cn[c0].push_back(c1);
+      cn[c1].push_back(c0);
+    } else {
+      cn[c0].push_back(c0);
+    }
+  }
+  M.cell_ptr.assign(1, 0);
+  for (int c = 0; c < nC; ++c) {
+    if (cf[c].empty()) {
+      *err = "cell without faces";
+      return kEMesh;
+    }
+    M.cell_faces.insert(M.cell_faces.end(), cf[c].begin(), cf[c].end());
+    M.cell_nb.insert(M.cell_nb.end(), cn[c].begin(), cn[c].end());
+    M.cell_ptr.push_back((int)M.cell_faces.size());
+  }
+  // Face::setCenter (Face.cpp:8-39): centre = mean of nodes; area vector
+  // 0.5 (n1-n0) x (n2-n0) for triangles, (n1-n0) x (n2-n0) for quads
+  M.face_ctr.assign(3 * (size_t)nF, 0.0);
+  M.face_dir.assign(3 * (size_t)nF, 0.0);
+  M.face_area.assign(nF, 0.0);
+  for (int f = 0; f < nF; ++f) {
+    const int b0 = M.face_ptr[f], k = M.face_ptr[f + 1] - b0;
+    double sm[3] = {0, 0, 0};
+    for (int j = 0; j < k; ++j)
+      for (int d = 0; d < 3; ++d) sm[d] += M.node_xyz[3 * (size_t)M.face_nodes[b0 + j] + d];
+    for (int d = 0; d < 3; ++d) M.face_ctr[3 * (size_t)f + d] = sm[d] / (double)k;
+    const double* p0 = &M.node_xyz[3 * (size_t)M.face_nodes[b0]];
+    const double* p1 = &M.node_xyz[3 * (size_t)M.face_nodes[b0 + 1]];
+    const double* p2 = &M.node_xyz[3 * (size_t)M.face_nodes[b0 + 2]];
+    double f1[3], f2[3], cr[3];
+    sub3(p1, p0, f1);
+    sub3(p2, p0, f2);
+    cr[0] = f1[1] * f2[2] - f1[2] * f2[1];
+    cr[1] = f1[2] * f2[0] - f1[0] * f2[2];
+    cr[2] = f1[0] * f2[1] - f1[1] * f2[0];
+    double* dv = &M.face_dir[3 * (size_t)f];
+    for (int d = 0; d < 3; ++d) dv[d] = (k == 3) ? 0.5 * cr[d] : cr[d];
+    M.face_area[f] = norm3(dv);
+  }
+  // Cell::setCenter (mean of face centres) and setVolume (Cell.cpp:52-59,
+  // the reference's 3D formula: sum of area (c - x_f) . n_f/|n_f| with the
+  // stored face direction), and the corrected volume
+  // V = 1/3 sum (x_f - c) . S_f(outward)
+  M.cell_ctr.assign(3 * (size_t)nC, 0.0);
+  M.cell_vol.assign(nC, 0.0);
+  M.cell_vol_fixed.assign(nC, 0.0);
+  for (int c = 0; c < nC; ++c) {
+    double sm[3] = {0, 0, 0};
+    const int kb = M.cell_ptr[c], ke = M.cell_ptr[c + 1];
+    for (int k = kb; k < ke; ++k)
+      for (int d = 0; d < 3; ++d) sm[d] += M.face_ctr[3 * (size_t)M.cell_faces[k] + d];
+    double* cc = &M.cell_ctr[3 * (size_t)c];
+    for (int d = 0; d < 3; ++d) cc[d] = sm[d] / (double)(ke - kb);
+    double vol = 0, vfix = 0;
+    for (int k = kb; k < ke; ++k) {
+      const int f = M.cell_faces[k];
+      const double* dv = &M.face_dir[3 * (size_t)f];
+      const double nrm = norm3(dv);
+      double u[3], tv[3];
+      for (int d = 0; d < 3; ++d) u[d] = dv[d] / nrm;
+      sub3(cc, &M.face_ctr[3 * (size_t)f], tv);
+      double at[3];
+      for (int d = 0; d < 3; ++d) at[d] = M.face_area[f] * tv[d];
+      vol += dot3(at, u);
+      // corrected: the face's area vector pointed out of this cell
+      double xf[3];
+      sub3(&M.face_ctr[3 * (size_t)f], cc, xf);
+      double s = dot3(xf, dv);
+      vfix += std::fabs(s);
+    }
+    M.cell_vol[c] = vol;
+    M.cell_vol_fixed[c] = vfix / 3.0;
+  }
+  // orientation (MshBlock.cpp:632-648): where the area vector points into
+  // c0 the face flips directAndCells and sets its left/right flags
+  M.face_dac.assign(nF, 1);
+  M.face_flag.assign(3 * (size_t)nF, 0);
+  M.face_flag_set.assign(nF, 0);
+  for (int f = 0; f < nF; ++f) {
+    const double* dv = &M.face_dir[3 * (size_t)f];
+    double t[3];
+    sub3(&M.face_ctr[3 * (size_t)f], &M.cell_ctr[3 * (size_t)M.face_cells[2 * f]], t);
+    if (dot3(dv, t) < 0) {
+      M.face_dac[f] = -1;
+      M.face_flag_set[f] = 1;
+      for (int d = 0; d < 3; ++d) M.face_flag[3 * (size_t)f + d] = (-1 * dv[d] >= 0) ? 1 : 0;
+    }
+  }
+  // directOfNbFaces, eta0, centre-middle difference, eta0C
+  const int tot = M.cell_ptr[nC];
+  M.cell_dof.assign(3 * (size_t)tot, 0.0);
+  M.cell_eta0c.assign(tot, 0.0);
+  M.face_eta0.assign(nF, 1.0);
+  M.face_cmd.assign(3 * (size_t)nF, 0.0);
+  for (int c = 0; c < nC; ++c)
+    for (int k = M.cell_ptr[c]; k < M.cell_ptr[c + 1]; ++k) {
+      const int f = M.cell_faces[k];
+      const double s = (M.face_cells[2 * f] == c) ? M.face_dac[f] : -M.face_dac[f];
+      for (int d = 0; d < 3; ++d) M.cell_dof[3 * (size_t)k + d] = s * M.face_dir[3 * (size_t)f + d];
+    }
+  for (int f = 0; f < nF; ++f) {
+    const int c0 = M.face_cells[2 * f], c1 = M.face_cells[2 * f + 1];
+    if (c1 >= 0) {
+      double a[3], bb[3];
+      sub3(&M.cell_ctr[3 * (size_t)c1], &M.face_ctr[3 * (size_t)f], a);
+      sub3(&M.cell_ctr[3 * (size_t)c0], &M.face_ctr[3 * (size_t)f], bb);
+      const double n1 = norm3(a);
+      M.face_eta0[f] = n1 / (norm3(bb) + n1);
+    }
+  }
+  for (int f = 0; f < M.n_int_faces && f < nF; ++f) {
+    const int c0 = M.face_cells[2 * f], c1 = M.face_cells[2 * f + 1];
+    if (c1 < 0) continue;
+    for (int d = 0; d < 3; ++d) {
+      const double mid = 0.5 * (M.cell_ctr[3 * (size_t)c0 + d] + M.cell_ctr[3 * (size_t)c1 + d]);
+      M.face_cmd[3 * (size_t)f + d] = M.face_ctr[3 * (size_t)f + d] - mid;
+    }
+  }
+  for (int c = 0; c < nC; ++c)
+    for (int k = M.cell_ptr[c]; k < M.cell_ptr[c + 1]; ++k) {
+      const int f = M.cell_faces[k];
+      M.cell_eta0c[k] = (M.face_cells[2 * f] == c) ? M.face_eta0[f] : 1 - M.face_eta0[f];
+    }
+  // cell nodes (MshBlock.cpp:681-723): first appearance over the faces;
+  // a 4-node cell is reordered by the angles at node 0
+  M.cell_node_ptr.assign(1, 0);
+  for (int c = 0; c < nC; ++c) {
+    const size_t base = M.cell_nodes.size();
+    for (int k = M.cell_ptr[c]; k < M.cell_ptr[c + 1]; ++k) {
+      const int f = M.cell_faces[k];
+      for (int j = M.face_ptr[f]; j < M.face_ptr[f + 1]; ++j) {
+        const int nd = M.face_nodes[j];
+        bool have = false;
+        for (size_t i = base; i < M.cell_nodes.size(); ++i) have = have || M.cell_nodes[i] == nd;
+        if (!have) M.cell_nodes.push_back(nd);
+      }
+    }
+    if (M.cell_nodes.size() - base == 4) {
+      int* p = &M.cell_nodes[base];
+      double v1[3], v2[3], v3[3];
+      sub3(&M.node_xyz[3 * (size_t)p[1]], &M.node_xyz[3 * (size_t)p[0]], v1);
+      sub3(&M.node_xyz[3 * (size_t)p[2]], &M.node_xyz[3 * (size_t)p[0]], v2);
+      sub3(&M.node_xyz[3 * (size_t)p[3]], &M.node_xyz[3 * (size_t)p[0]], v3);
+      const double a12 = std::acos(dot3(v1, v2) / (norm3(v1) * norm3(v2)));
+      const double a23 = std::acos(dot3(v3, v2) / (norm3(v3) * norm3(v2)));
+      const double a13 = std::acos(dot3(v1, v3) / (norm3(v1) * norm3(v3)));
+      if (a13 < a12 || a13 < a23) {
+        if (a12 > a23) std::swap(p[2], p[3]);
+        else std::swap(p[1], p[2]);
+      }
+    }
+    M.cell_node_ptr.push_back((int)M.cell_nodes.size());
+  }
+  // boundary lists (as the 2D reader: MshBlock.cpp:727-743) and the count
+  // of lower-id neighbours (:746-756)
+  std::vector<uint8_t> bflag(nC, 0);
+  for (int f = 0; f < nF; ++f)
+    if (M.face_cells[2 * f + 1] < 0) {
+      const int c0 = M.face_cells[2 * f];
+      if (!bflag[c0]) {
+        M.bond1.push_back(c0);
+        bflag[c0] = 1;
+      }
+    }
+  for (int c1 : M.bond1)
+    for (int k = M.cell_ptr[c1]; k < M.cell_ptr[c1 + 1]; ++k) {
+      const int nb = M.cell_nb[k];
+      if (!bflag[nb]) {
+        M.bond2.push_back(nb);
+        bflag[nb] = 1;
+      }
+    }
+  for (int c = 0; c < nC; ++c)
+    if (!bflag[c]) M.inner.push_back(c);
+  M.cell_nL.assign(nC, 0);
+  for (int c = 0; c < nC; ++c)
+    for (int k = M.cell_ptr[c]; k < M.cell_ptr[c + 1]; ++k) M.cell_nL[c] += (c > M.cell_nb[k]);
+  return kOk;
+}
 }  // namespace mst

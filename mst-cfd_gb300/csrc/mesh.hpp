@@ -45,6 +45,31 @@ struct HostMesh {
   int n_zones() const { return (int)zone.size() / 4; }
 };
 
+// A 3D mesh as MshBlock reads it with DIM 3 (mesh/MshBlock.cpp:436-789):
+// triangular and quadrilateral faces (zones with a fixed node count, or
+// mixed zones whose lines start with their node count), geometry by the
+// reference's 3D formulas (Face.cpp:20-39, Cell.cpp:6-14 and :52-59), plus
+// the corrected cell volume by the divergence theorem.
+struct HostMesh3D {
+  int n_nodes = 0, n_cells = 0, n_faces = 0, n_int_faces = 0;
+  std::vector<int> zone;          // [nz][4] id, first, last, type
+  std::vector<double> node_xyz;   // [nN][3]
+  std::vector<int> face_ptr;      // [nF+1] into face_nodes
+  std::vector<int> face_nodes;    // node ids of each face, in file order
+  std::vector<int> face_cells;    // [nF][2], c1 = -1 on boundary
+  std::vector<int> face_type;     // [nF]
+  std::vector<double> face_ctr, face_dir, face_area, face_eta0, face_cmd;  // cmd: [nF][3]
+  std::vector<int> face_dac;
+  std::vector<uint8_t> face_flag;      // [nF][3] flagLeftRight where set
+  std::vector<uint8_t> face_flag_set;  // [nF] 1 where the reference sets them
+  std::vector<int> cell_ptr, cell_faces, cell_nb;
+  std::vector<double> cell_dof, cell_eta0c, cell_ctr, cell_vol, cell_vol_fixed;
+  std::vector<int> cell_node_ptr, cell_nodes;  // reader's node order
+  std::vector<int> inner, bond1, bond2;
+  std::vector<int> cell_nL;  // [nC] neighbours with a lower id (MshBlock.cpp:746-756)
+};
+int read_msh3d(const std::string& path, HostMesh3D* m, std::string* err);
+
 // Status codes shared with the C ABI.
 enum : int { kOk = 0, kEInval = 1, kEMesh = 2 };
 

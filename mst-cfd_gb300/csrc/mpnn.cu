@@ -216,6 +216,7 @@ struct mst_mpnn {
   __nv_bfloat16 *dPb = nullptr, *tA = nullptr, *tB = nullptr, *dYb = nullptr, *WdT = nullptr,
                 *WlT = nullptr;
   float* part = nullptr;  // split-K partial products of the weight gradients
+  float* feat = nullptr;  // the graph's FP32 features [cap][16]
   int *ptr = nullptr, *nbr = nullptr;
   int n_nbr_cap = 0;
   int n = 0;  // cells of the current graph
@@ -275,6 +276,7 @@ cudaError_t ensure_cap(mst_mpnn* m, int n, int n_nbr) {
   if (e == cudaSuccess) e = nalloc(m, &m->WdT, (size_t)kW * kInK);
   if (e == cudaSuccess) e = nalloc(m, &m->WlT, (size_t)kZ * kW);
   if (e == cudaSuccess) e = nalloc(m, &m->part, (size_t)kMaxSplits * kW * kZ);
+  if (e == cudaSuccess) e = nalloc(m, &m->feat, (size_t)n * kIn);
   return e;
 }
 
@@ -512,8 +514,7 @@ mst_status mst_mpnn_set_graph(mst_mpnn* m, int n, const float* features, const i
   for (int i = 0; i < n_nbr; ++i)
     if (nbr[i] < 0 || nbr[i] >= n) return mst_internal_fail(MST_EINVAL, "neighbour id out of range");
   cudaError_t e = ensure_cap(m, n, std::max(n_nbr, 1));
-  float* df = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(float) * (size_t)n * kIn);
+  float* df = m->feat;
   if (e == cudaSuccess)
     e = cudaMemcpy(df, features, sizeof(float) * (size_t)n * kIn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -527,7 +528,6 @@ mst_status mst_mpnn_set_graph(mst_mpnn* m, int n, const float* features, const i
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  cudaFree(df);
   if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn graph: ") + cudaGetErrorString(e));
   m->n = n;
   return MST_OK;

@@ -40,6 +40,23 @@ class MeshDesc(C.Structure):
                 ("n_zones", C.c_int), ("zones", _ip), ("c1_shift", _dp)]
 
 
+class Mesh3DInfo(C.Structure):
+    _fields_ = [(k, C.c_int) for k in (
+        "n_nodes", "n_cells", "n_faces", "n_int_faces", "n_zones", "n_face_nodes",
+        "n_cell_faces", "n_cell_nodes", "n_inner", "n_bond1", "n_bond2")]
+
+
+class Mesh3DArrays(C.Structure):
+    _fields_ = [("node_xyz", _dp), ("face_ptr", _ip), ("face_nodes", _ip), ("face_cells", _ip),
+                ("face_type", _ip), ("face_ctr", _dp), ("face_dir", _dp), ("face_area", _dp),
+                ("face_eta0", _dp), ("face_cmd", _dp), ("face_dac", _ip), ("face_flag", _up),
+                ("face_flag_set", _up), ("cell_ptr", _ip), ("cell_faces", _ip),
+                ("cell_nb", _ip), ("cell_dof", _dp), ("cell_eta0c", _dp), ("cell_ctr", _dp),
+                ("cell_vol", _dp), ("cell_vol_fixed", _dp), ("cell_node_ptr", _ip),
+                ("cell_nodes", _ip), ("inner", _ip), ("bond1", _ip), ("bond2", _ip),
+                ("cell_n_lower", _ip)]
+
+
 class CaseParams(C.Structure):
     _fields_ = [("inlet_q", C.c_double * 4), ("mu", C.c_double), ("lambda_", C.c_double),
                 ("kappa", C.c_double), ("cv", C.c_double)]
@@ -174,6 +191,10 @@ def load():
         "mst_mpnn_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
         "mst_mpnn_set_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
         "mst_mpnn_adam_step": (C.c_int, [C.c_void_p, C.c_float]),
+        "mst_mesh3d_read_msh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+        "mst_mesh3d_get_info": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DInfo)]),
+        "mst_mesh3d_get_arrays": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DArrays)]),
+        "mst_mesh3d_destroy": (None, [C.c_void_p]),
         "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
                                     C.POINTER(C.c_void_p)]),
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),

@@ -348,6 +348,145 @@ def write_msh(path, mesh, crlf=False):
 
 
 # ---------------------------------------------------------------------------
+# 3D meshes (host reader only)
+# ---------------------------------------------------------------------------
+_KUHN = [(0, 1, 3, 7), (0, 1, 5, 7), (0, 2, 3, 7), (0, 2, 6, 7), (0, 4, 5, 7), (0, 4, 6, 7)]
+_HEX_FACES = [(0, 2, 6, 4), (1, 3, 7, 5), (0, 1, 5, 4), (2, 3, 7, 6), (0, 1, 3, 2), (4, 5, 7, 6)]
+
+
+def _box_nodes(nx, ny, nz, length, jitter, seed):
+    rng = np.random.default_rng(seed)
+    h = length / np.array([nx, ny, nz], float)
+    g = np.stack(np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1),
+                             indexing="ij"), -1).reshape(-1, 3).astype(float)
+    inner = np.all((g > 0) & (g < [nx, ny, nz]), 1)
+    j = rng.uniform(-jitter, jitter, g.shape) * inner[:, None]
+    xyz = (g + j) * h
+    idx = lambda i, k, l: (i * (ny + 1) + k) * (nz + 1) + l
+    return xyz, idx
+
+
+def _assemble3d(xyz, cells_faces, n_cells, side_of, kinds):
+    """Unique faces of the cells (node tuples per cell face), boundary faces
+    grouped by box side; every area vector points into c0."""
+    keys = {}
+    faces, fc = [], []
+    for c, fl in enumerate(cells_faces):
+        for f in fl:
+            k = tuple(sorted(f))
+            if k in keys:
+                fc[keys[k]][1] = c
+            else:
+                keys[k] = len(faces)
+                faces.append(list(f))
+                fc.append([c, -1])
+    fc = np.array(fc)
+    cen = np.zeros((n_cells, 3))
+    cnt = np.zeros(n_cells)
+    for f, (a, b) in zip(faces, fc):
+        m = xyz[f].mean(0)
+        for cc in (a, b):
+            if cc >= 0:
+                cen[cc] += m
+                cnt[cc] += 1
+    cen /= cnt[:, None]
+    # orient into c0: the reference's area vector (n1-n0) x (n2-n0)
+    for i, f in enumerate(faces):
+        p = xyz[f]
+        d = np.cross(p[1] - p[0], p[2] - p[0])
+        if np.dot(d, p.mean(0) - cen[fc[i, 0]]) > 0:
+            faces[i] = f[::-1]
+    interior = fc[:, 1] >= 0
+    side = np.array([side_of(xyz[f].mean(0)) if not interior[i] else -1
+                     for i, f in enumerate(faces)])
+    groups = [np.where(interior)[0]] + [np.where(side == s)[0] for s in range(6)]
+    types = [INTERIOR] + list(kinds)
+    order = np.concatenate(groups)
+    zones, start = [], 1
+    for zi, (g, ty) in enumerate(zip(groups, types)):
+        if len(g):
+            zones.append((zi + 1, start, start + len(g) - 1, ty))
+            start += len(g)
+    return dict(node_xyz=xyz, faces=[faces[i] for i in order], face_cells=fc[order],
+                zones=np.array(zones, np.int32), n_cells=n_cells)
+
+
+def tet_box(n=4, length=1.0, jitter=0.15, seed=1,
+            kinds=(INLET, OUTLET, WALL, WALL, SYMMETRY, SYMMETRY)):
+    """n^3 jittered hexahedra split into 6 tetrahedra each (the config-3
+    mesh type), one boundary zone per box side (x-, x+, y-, y+, z-, z+)."""
+    xyz, idx = _box_nodes(n, n, n, length, jitter, seed)
+    cells = []
+    for i in range(n):
+        for k in range(n):
+            for l in range(n):
+                v = [idx(i + (c & 1), k + ((c >> 1) & 1), l + ((c >> 2) & 1)) for c in range(8)]
+                for t in _KUHN:
+                    q = [v[j] for j in t]
+                    cells.append([[q[0], q[1], q[2]], [q[0], q[1], q[3]], [q[0], q[2], q[3]],
+                                  [q[1], q[2], q[3]]])
+    tol = 1e-9 * length
+
+    def side_of(c):
+        for d in range(3):
+            if abs(c[d]) < tol:
+                return 2 * d
+            if abs(c[d] - length) < tol:
+                return 2 * d + 1
+        raise RuntimeError("boundary face off the box")
+    return _assemble3d(xyz, cells, len(cells), side_of, kinds)
+
+
+def hex_box(n=4, length=1.0, jitter=0.0, seed=1,
+            kinds=(INLET, OUTLET, WALL, WALL, SYMMETRY, SYMMETRY)):
+    """n^3 hexahedra (quadrilateral faces), one boundary zone per side."""
+    xyz, idx = _box_nodes(n, n, n, length, jitter, seed)
+    cells = []
+    for i in range(n):
+        for k in range(n):
+            for l in range(n):
+                v = [idx(i + (c & 1), k + ((c >> 1) & 1), l + ((c >> 2) & 1)) for c in range(8)]
+                cells.append([[v[j] for j in f] for f in _HEX_FACES])
+    tol = 1e-9 * length
+
+    def side_of(c):
+        for d in range(3):
+            if abs(c[d]) < tol:
+                return 2 * d
+            if abs(c[d] - length) < tol:
+                return 2 * d + 1
+        raise RuntimeError("boundary face off the box")
+    return _assemble3d(xyz, cells, len(cells), side_of, kinds)
+
+
+def write_msh3d(path, mesh, mixed_zones=(), crlf=False):
+    """Fluent ASCII 3D .msh: zones with a fixed face node count, or, for the
+    zone indices in mixed_zones, a mixed zone (node count 0 in the header,
+    each line led by its node count)."""
+    nl = "\r\n" if crlf else "\n"
+    xyz, faces, fc, zones = mesh["node_xyz"], mesh["faces"], mesh["face_cells"], mesh["zones"]
+    nN, nF, nC = len(xyz), len(faces), int(mesh["n_cells"])
+    out = ['(0 "mstcfd meshgen 3D")', "(2 3)",
+           f"(10 (0 1 {nN:x} 0 3))", f"(10 (1 1 {nN:x} 1 3)", "("]
+    out += [f"{x!r} {y!r} {z!r}" for x, y, z in xyz.tolist()]
+    out += ["))", f"(12 (0 1 {nC:x} 0 0))", f"(12 (2 1 {nC:x} 1 0))",
+            f"(13 (0 1 {nF:x} 0 0))"]
+    for zi, (zid, st, en, ty) in enumerate(zones.tolist()):
+        k = len(faces[st - 1])
+        mixed = zi in mixed_zones
+        out.append(f'(0 "zone {zi}")')
+        out.append(f"(13 ({zid + 2:x} {st:x} {en:x} {ty:x} {0 if mixed else k:x})(")
+        for f in range(st - 1, en):
+            ids = " ".join(f"{v + 1:x}" for v in faces[f])
+            c0, c1 = fc[f] + 1
+            lead = f"{len(faces[f]):x} " if mixed else ""
+            out.append(f"{lead}{ids} {c0:x} {c1 if c1 > 0 else 0:x}")
+        out.append("))")
+    with open(path, "w", newline="") as fh:
+        fh.write(nl.join(out) + nl)
+
+
+# ---------------------------------------------------------------------------
 # initial states
 # ---------------------------------------------------------------------------
 def reference_inlet():

@@ -1,0 +1,103 @@
+"""Accuracy statements of the benchmark configurations, run on the GPU.
+
+  python -m mstcfd.validate vortex [--n 1000] [--periods 10] [--fp64-periods 10]
+
+Isentropic vortex (strength 5, Mach 0.5) on the periodic jittered Delaunay
+mesh, AUSM+ + van Leer, RK2 at CFL 0.5: the FP32 and FP64 paths advanced
+the same number of periods, with the L2 and L-infinity density errors of the
+FP32 path against the FP64 path and of both against the analytic solution
+(the vortex convected back to its start).  One JSON line.
+
+  python -m mstcfd.validate sod
+
+Sod tube, 1000x4 quads, Roe + minmod, RK2 at CFL 0.5 to t = 0.2: the FP64
+and FP32 paths against the exact Riemann solution (L1, L2, L-infinity of
+density).
+"""
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+
+def _errors(a, b):
+    d = a - b
+    return {"l2": float(np.sqrt(np.mean(d * d))), "linf": float(np.abs(d).max())}
+
+
+def vortex(n=1000, periods=10.0, fp64_periods=None, cfl=0.5):
+    from . import Mesh, Solver
+    from . import meshgen as mg
+    m = mg.periodic_delaunay(n, 10.0, jitter=0.25, seed=20261203)
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"], c1_shift=m["c1_shift"])
+    xy = m["cell_centroid"]
+    q0 = mg.isentropic_vortex(xy)
+    period = 10.0 / (0.5 * np.sqrt(1.4))
+    out = {"workload": f"isentropic vortex, {m['n_cells']} triangles, AUSM+ + van Leer, "
+                       f"RK2, CFL {cfl}", "periods": {}}
+    fp64_periods = periods if fp64_periods is None else fp64_periods
+    res = {}
+    for prec, label, nper in ((2, "fp32", periods), (1, "fp64", fp64_periods)):
+        s = Solver(mesh, flux=0, order=2, limiter=2, reference_quirks=0, time_scheme=1,
+                   dt_mode=1, cfl=cfl, precision=prec)
+        s.set_state(q0)
+        t_end = nper * period
+        t0 = time.perf_counter()
+        steps = 0
+        while s.time() < t_end - 1e-12:
+            s.step(500, t_end=t_end)
+            steps += 500
+        res[label] = (s.state(), time.perf_counter() - t0, s.time())
+        out["periods"][label] = nper
+        s.close()
+    exact = q0  # after whole periods the vortex is back at its start
+    for label, (q, secs, t) in res.items():
+        out[label] = {"vs_analytic": _errors(q[:, 0], exact[:, 0]), "wall_s": round(secs, 1),
+                      "time": t}
+    if periods == fp64_periods:
+        out["fp32_vs_fp64"] = _errors(res["fp32"][0][:, 0], res["fp64"][0][:, 0])
+    return out
+
+
+def sod():
+    from . import Mesh, Solver
+    from . import meshgen as mg
+    from .analytic import riemann_sample
+    m = mg.sod_strip(1000, 4, ends=mg.OUTLET)
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"])
+    x = mesh.arrays()["cell_ctr"][:, 0]
+    rho_e, _, _ = riemann_sample(x, 0.2, 0.5, (1.0, 0.0, 1.0), (0.125, 0.0, 0.1))
+    out = {"workload": "Sod tube, 1000x4 quads, Roe + minmod, RK2, CFL 0.5, t = 0.2"}
+    for prec, label in ((1, "fp64"), (2, "fp32")):
+        s = Solver(mesh, flux=1, order=2, limiter=1, reference_quirks=0, time_scheme=1,
+                   dt_mode=1, cfl=0.5, precision=prec)
+        s.set_state(mg.sod_state(mesh.arrays()["cell_ctr"]))
+        while s.time() < 0.2 - 1e-15:
+            s.step(100, t_end=0.2)
+        rho = s.state()[:, 0]
+        e = _errors(rho, rho_e)
+        e["l1"] = float(np.mean(np.abs(rho - rho_e)))
+        out[label] = e
+        s.close()
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["vortex", "sod"])
+    ap.add_argument("--n", type=int, default=1000)
+    ap.add_argument("--periods", type=float, default=10.0)
+    ap.add_argument("--fp64-periods", type=float, default=None)
+    a = ap.parse_args(argv)
+    if a.case == "vortex":
+        print(json.dumps(vortex(a.n, a.periods, a.fp64_periods)))
+    else:
+        print(json.dumps(sod()))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -46,9 +46,10 @@ def build_ref(force=False):
     sources are not present on this machine."""
     if not ref_available():
         return False
-    marker = os.path.join(REF_OUT, "ref_io")
+    marker = os.path.join(REF_OUT, "ref_mesh3d")
     deps = [os.path.join(HERE, "ref", f) for f in
             ("build_ref.sh", "harness_rho.cpp", "harness_lu.cpp", "harness_io.cpp",
+             "harness_mesh3d.cpp",
              os.path.join("eigen_shim", "Eigen", "shim_matrix.h"))]
     if force or _stale(marker, deps):
         env = dict(os.environ, MSTCFD_REF_SRC=REF_SRC, MSTCFD_REF_OUT=REF_OUT)

@@ -100,9 +100,26 @@ objs=""
 for f in $SRCS; do objs="$objs $O/$(echo "$f" | tr '/' '_').o"; done
 $CXX $CXXFLAGS $objs "$O/work_Work.cpp.o" "$O/harness_io.o" -o "$OUT/ref_io"
 
+# 3D reader: the mesh sources with DIM 3 (harness_mesh3d.cpp)
+mirror mesh3d 1 SolverAusm
+printf '#undef DIM\n#define DIM 3\n' >> "$OUT/mesh3d/src/include/CONST.h"
+S3="$OUT/mesh3d/src"
+O3="$OUT/mesh3d/obj"
+mkdir -p "$O3"
+objs3=""
+for f in mesh/Cell.cpp mesh/Face.cpp mesh/Node.cpp mesh/FacesInf.cpp mesh/MshBlock.cpp work/FUNCTION.cpp; do
+  o="$O3/$(echo "$f" | tr '/' '_').o"
+  objs3="$objs3 $o"
+  $CXX $CXXFLAGS -I"$S3" -c "$S3/$f" -o "$o" &
+done
+$CXX $CXXFLAGS -I"$S3" -c "$HERE/harness_mesh3d.cpp" -o "$O3/harness_mesh3d.o" &
+wait
+$CXX $CXXFLAGS $objs3 "$O3/harness_mesh3d.o" -o "$OUT/ref_mesh3d"
+
 for v in ausm_o1 ausm_o2 roe_o1 roe_o2; do
   test -x "$OUT/ref_rho_$v"
 done
+test -x "$OUT/ref_mesh3d"
 test -x "$OUT/ref_lu"
 test -x "$OUT/ref_io"
 echo "build_ref: ok ($OUT)"

@@ -133,3 +133,23 @@ def run_io(mesh_path, q, zone_t=0, time_now=0):
         cell = f.read()
     back = np.fromfile(os.path.join(d, "readback.bin"), dtype=np.float64).reshape(-1, 4)
     return plt, cell, back
+
+
+def run_mesh3d(mesh_path):
+    """The reference's 3D reader (oracle/ref/harness_mesh3d.cpp): dict of
+    its arrays."""
+    if not _build.build_ref():
+        raise RuntimeError("reference sources not available")
+    d = tempfile.mkdtemp(prefix="mst3d_")
+    subprocess.run([os.path.join(_build.REF_OUT, "ref_mesh3d"), os.path.abspath(mesh_path), d],
+                   check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    spec = {"counts": np.int32, "node_xyz": np.float64, "face_ctr": np.float64,
+            "face_dir": np.float64, "face_area": np.float64, "face_eta0": np.float64,
+            "face_cmd": np.float64, "face_dac": np.int32, "face_flag": np.uint8,
+            "face_cells": np.int32, "face_ptr": np.int32, "face_nodes": np.int32,
+            "cell_ctr": np.float64, "cell_vol": np.float64, "cell_ptr": np.int32,
+            "cell_faces": np.int32, "cell_nb": np.int32, "cell_dof": np.float64,
+            "cell_eta0c": np.float64, "cell_node_ptr": np.int32, "cell_nodes": np.int32,
+            "cell_nlow": np.int32, "inner": np.int32, "bond1": np.int32, "bond2": np.int32}
+    ext = {np.int32: "i32", np.float64: "f64", np.uint8: "u8"}
+    return {k: np.fromfile(os.path.join(d, f"{k}.{ext[t]}"), dtype=t) for k, t in spec.items()}
