@@ -157,6 +157,48 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _tensor_peak():
+    """Burst dense BF16 TFLOP/s (the GEMMs are timed alone)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def _gemm_at_scale(net, feats):
+    """One forward + backward of the network over the union of the batch's
+    graphs with every tensor-core GEMM launch timed by CUDA events: achieved
+    TFLOP/s (2MNK) and GB/s (operands + results) against the measured
+    peaks."""
+    from mstcfd import warmstart as ws
+    fu, pu, nu, _ = ws.union([(f, ptr, nbr, None) for f, ptr, nbr, _ in feats])
+    net.set_graph(fu, pu, nu)
+    net.set_targets(np.zeros((len(fu), 4), np.float32))
+    net.forward()
+    net.backward()  # warm-up
+    net.profile(True)
+    t0 = time.perf_counter()
+    net.forward()
+    net.backward()
+    step_s = time.perf_counter() - t0
+    g = net.profile_read()
+    net.profile(False)
+    tf_peak, tf_src = _tensor_peak()
+    hbm, hbm_src = _peaks()
+    tflops = g["flops"] / (g["ms"] * 1e-3) / 1e12
+    gbs = g["bytes"] / (g["ms"] * 1e-3) / 1e9
+    ridge = tf_peak * 1e12 / (hbm * 1e9)
+    return {"cells": int(len(fu)), "train_step_s": round(step_s, 4),
+            "gemm_launches": g["launches"], "gemm_ms": round(g["ms"], 3),
+            "gemm_share_of_step": round(g["ms"] * 1e-3 / step_s, 3),
+            "tflops": round(tflops, 2), "tensor_frac": round(tflops / tf_peak, 4),
+            "tensor_peak": tf_peak, "tensor_peak_source": tf_src,
+            "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4), "hbm_peak_source": hbm_src,
+            "flops_per_byte": round(g["flops"] / g["bytes"], 1), "ridge_flops_per_byte": round(ridge, 1),
+            "bound": "hbm" if g["flops"] / g["bytes"] < ridge else "tensor"}
+
+
 def _profile_traffic(kernel, n_cells):
     """DRAM bytes per launch of ``kernel`` from the committed ncu summary
     (per cell, scaled to this mesh), or None."""
@@ -384,6 +426,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
     t2 = time.perf_counter()
     q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
     infer_s = time.perf_counter() - t2
+    gemm = _gemm_at_scale(net, feats)
     b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q_warm)
@@ -420,7 +463,8 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
                       "seeds": "disjoint from the batch", "steps": args.warm_steps,
                       "loss_first": round(float(hist[0]), 5),
                       "loss_last": round(float(hist[-20:].mean()), 5),
-                      "data_s": round(data_s, 2), "train_s": round(train_s, 2)}}
+                      "data_s": round(data_s, 2), "train_s": round(train_s, 2)},
+            "network_gemm": gemm}
 
 
 def run_cpu_sample(m, steps, budget_s=30.0):

@@ -401,6 +401,14 @@ mst_status mst_mpnn_get(mst_mpnn *m, int which, float *out);
 mst_status mst_mpnn_set_weights(mst_mpnn *m, const float *w);
 /* One Adam step (beta 0.9 / 0.999) with the current gradients. */
 mst_status mst_mpnn_adam_step(mst_mpnn *m, float lr);
+/* Live timing of the network's tensor-core GEMM launches: on != 0 starts
+ * recording (a CUDA event pair around every GEMM launch), 0 stops; both
+ * clear what was recorded.  profile_read synchronises the device and
+ * returns out[0] = summed GEMM milliseconds, out[1] = their 2MNK flops,
+ * out[2] = their operand and result bytes, out[3] = launches, then clears
+ * the record.  No reference counterpart (the reference has no network). */
+mst_status mst_mpnn_profile(mst_mpnn *m, int on);
+mst_status mst_mpnn_profile_read(mst_mpnn *m, double out[4]);
 
 /* ------------------------------------------------------------------ */
 /* result writer and checkpoint files                                  */

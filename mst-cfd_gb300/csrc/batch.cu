@@ -174,6 +174,7 @@ mst::LusgsArgs sweep_args(mst_batch* b, int which) {
   la.viscous = c->p.viscous;
   la.omega = b->ip.omega;
   la.conv_iter = b->conv_iter;
+  la.iter = b->iter;
   return la;
 }
 
@@ -437,6 +438,9 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
     cleanup();
     return st;
   }
+  // the residual kernels skip the cells of converged cases
+  b->ctx->dm.c_case = b->c_case;
+  b->ctx->dm.case_conv = b->conv_iter;
   if (cudaStreamSynchronize(b->ctx->stream) != cudaSuccess) {
     cleanup();
     return mst_internal_fail(MST_ECUDA, "batch setup failed");

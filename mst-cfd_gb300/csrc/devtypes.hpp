@@ -38,7 +38,27 @@ struct DevMesh {
   const int* t_own_ptr;
   const int* t_bor_ptr;
   const int* t_bor;
+  // batches (nullptr for a single mesh): the case of every device cell and
+  // the iteration at which each case converged (-1 while it runs).  The
+  // residual kernels skip the cells of converged cases: after the
+  // iteration that converged them both state buffers hold the same state.
+  const int* c_case;
+  const int* case_conv;
 };
+
+// true when device cell c belongs to a converged case of a batch
+__device__ __forceinline__ bool cell_case_done(const DevMesh& m, int c) {
+  return m.case_conv && m.case_conv[m.c_case[c]] >= 0;
+}
+
+// true when every cell of [c0, c1) belongs to a converged case (the cases
+// are contiguous ranges of device cells)
+__device__ __forceinline__ bool range_cases_done(const DevMesh& m, int c0, int c1) {
+  if (!m.case_conv || c1 <= c0) return false;
+  for (int k = m.c_case[c0], e = m.c_case[c1 - 1]; k <= e; ++k)
+    if (m.case_conv[k] < 0) return false;
+  return true;
+}
 
 // Number of doubles of per-tile partial norms: linf[4], l2[4], mass.
 constexpr int kNormSlots = 9;
@@ -125,6 +145,7 @@ struct LusgsArgs {
   int viscous;
   double omega;
   const int* conv_iter;    // [n_cases] converged cases keep their state
+  const int* iter;         // iteration counter (already advanced by the norms)
 };
 
 // Per-case residual norms and the CFL of the next iteration, one block per

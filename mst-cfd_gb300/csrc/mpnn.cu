@@ -220,6 +220,16 @@ struct mst_mpnn {
   int *ptr = nullptr, *nbr = nullptr;
   int n_nbr_cap = 0;
   int n = 0;  // cells of the current graph
+  // live timing of the tensor-core GEMM launches (mst_mpnn_profile): one
+  // event pair per launch on the network's stream, with the launch's
+  // 2MNK flops and its operand/result bytes
+  struct GemmRec {
+    cudaEvent_t a = nullptr, b = nullptr;
+    double flops = 0.0, bytes = 0.0;
+  };
+  bool prof = false;
+  std::vector<GemmRec> recs;
+  size_t n_recs = 0;
 };
 
 namespace {
@@ -280,8 +290,31 @@ cudaError_t ensure_cap(mst_mpnn* m, int n, int n_nbr) {
   return e;
 }
 
+// brackets one GEMM launch with an event pair when profiling is on
+struct GemmTimer {
+  mst_mpnn* m;
+  mst_mpnn::GemmRec* r = nullptr;
+  GemmTimer(mst_mpnn* mm, double flops, double bytes) : m(mm) {
+    if (!m->prof) return;
+    if (m->n_recs == m->recs.size()) {
+      mst_mpnn::GemmRec g;
+      if (cudaEventCreate(&g.a) != cudaSuccess || cudaEventCreate(&g.b) != cudaSuccess) return;
+      m->recs.push_back(g);
+    }
+    r = &m->recs[m->n_recs++];
+    r->flops = flops;
+    r->bytes = bytes;
+    cudaEventRecord(r->a, 0);
+  }
+  ~GemmTimer() {
+    if (r) cudaEventRecord(r->b, 0);
+  }
+};
+
 cudaError_t gemm(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, float* C, int M,
                  int N, int K, int ldc, const float* bias, int relu, int acc) {
+  GemmTimer timer(m, 2.0 * M * N * K,
+                  2.0 * ((double)M * K + (double)N * K) + 4.0 * M * N * (acc ? 2 : 1));
   mst::tc::GemmArgs g{};
   g.A = A;
   g.B = B;
@@ -316,7 +349,12 @@ cudaError_t gemm_wgrad(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16*
   g.ldc = ldc;
   g.err = m->err;
   g.k_chunk = chunk;
-  cudaError_t e = mst::tc::gemm(g, 0);
+  cudaError_t e;
+  {
+    GemmTimer timer(m, 2.0 * M * N * K,
+                    2.0 * ((double)M * K + (double)N * K) + 4.0 * used * M * N);
+    e = mst::tc::gemm(g, 0);
+  }
   if (e != cudaSuccess) return e;
   const size_t mn = (size_t)M * ldc;
   mst::tc::k_reduce_splits<<<(unsigned)((mn + 255) / 256), 256>>>(m->part, used, mn, C);
@@ -500,7 +538,41 @@ mst_status mst_mpnn_destroy(mst_mpnn* m) {
   }
   for (void* p : m->bufs) cudaFree(p);
   cudaFree(m->nbr);
+  for (auto& r : m->recs) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
   delete m;
+  return MST_OK;
+}
+
+mst_status mst_mpnn_profile(mst_mpnn* m, int on) {
+  if (!m) return mst_internal_fail(MST_EINVAL, "NULL network");
+  m->prof = on != 0;
+  m->n_recs = 0;
+  return MST_OK;
+}
+
+mst_status mst_mpnn_profile_read(mst_mpnn* m, double out[4]) {
+  if (!m || !out) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess)
+    return mst_internal_fail(MST_ECUDA, std::string("mpnn profile: ") + cudaGetErrorString(e));
+  double ms = 0.0, fl = 0.0, by = 0.0;
+  for (size_t i = 0; i < m->n_recs; ++i) {
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, m->recs[i].a, m->recs[i].b);
+    if (e != cudaSuccess)
+      return mst_internal_fail(MST_ECUDA, std::string("mpnn profile: ") + cudaGetErrorString(e));
+    ms += t;
+    fl += m->recs[i].flops;
+    by += m->recs[i].bytes;
+  }
+  out[0] = ms;
+  out[1] = fl;
+  out[2] = by;
+  out[3] = (double)m->n_recs;
+  m->n_recs = 0;
   return MST_OK;
 }
 

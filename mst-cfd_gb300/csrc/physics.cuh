@@ -102,6 +102,66 @@ __host__ __device__ __forceinline__ void ausm_axis(const T ql[4], const AusmSide
   f[d + 1] += pF;
 }
 
+// The same AUSM+ quantities for the FP32 production path, with each
+// state's 1/rho computed once and the supersonic branches in closed form
+// ((M + |M|) / (2M) = 1 for M > 1, (M - |M|) = 0): fewer divisions, the
+// same formulas as ausm_axis (including the pressure polynomial whose
+// second term is not scaled by p) up to rounding.  Not used by the exact
+// path.
+struct AusmSideF {
+  float ir, p, a_face, a_true, fc[4];
+};
+
+__host__ __device__ __forceinline__ AusmSideF ausm_side_f(const float q[4]) {
+  AusmSideF s;
+  const float gm1 = Gas<float>::gm1();
+  s.ir = 1.0f / q[0];
+  const float m2 = q[1] * q[1] + q[2] * q[2];
+  s.p = (q[3] - 0.5f * m2 * s.ir) * gm1;
+  const float h = (q[3] + s.p) * s.ir;
+  const float as = sqrtf(h * (2.0f * gm1 / Gas<float>::gp1()));
+  const float U = sqrtf(m2) * s.ir;
+  s.a_face = as * as / fmaxf(as, U);
+  s.a_true = sqrtf(Gas<float>::gamma() * s.p * s.ir);
+  s.fc[0] = q[0];
+  s.fc[1] = q[1];
+  s.fc[2] = q[2];
+  s.fc[3] = q[3] + s.p;
+  return s;
+}
+
+__host__ __device__ __forceinline__ void ausm_axis_f(const float ql[4], const AusmSideF& L,
+                                                     const float qr[4], const AusmSideF& R, int d,
+                                                     float f[4]) {
+  const float iaF = 1.0f / fminf(R.a_face, L.a_face);
+  const float mL = ql[d + 1] * L.ir * iaF;
+  const float mR = qr[d + 1] * R.ir * iaF;
+  float mp, mm, pp, pm;
+  if (mL <= 1.0f) {
+    const float a = (mL + 1.0f) * (mL + 1.0f), b = (mL * mL - 1.0f) * (mL * mL - 1.0f);
+    mp = 0.25f * a + 0.125f * b;
+    pp = L.p * 0.25f * a * (2.0f - mL) + 0.1875f * mL * b;
+  } else {
+    mp = mL;
+    pp = L.p;
+  }
+  if (mR <= 1.0f) {
+    const float a = (mR - 1.0f) * (mR - 1.0f), b = (mR * mR - 1.0f) * (mR * mR - 1.0f);
+    mm = -0.25f * a - 0.125f * b;
+    pm = R.p * 0.25f * a * (2.0f + mR) - 0.1875f * mR * b;
+  } else {
+    mm = 0.0f;
+    pm = 0.0f;
+  }
+  const float mF = mm + mp, pF = pm + pp, amF = fabsf(mF);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float al = L.a_true * L.fc[k], ar = R.a_true * R.fc[k];
+    f[k] = 0.5f * (mF * (al + ar) - amF * (ar - al));
+  }
+  f[d + 1] += pF;
+}
+
 // AUSM+ flux of the split-axis scheme along axis d (0 = x, 1 = y).
 template <class T>
 __host__ __device__ __forceinline__ void ausm_flux(const T ql[4], const T qr[4],

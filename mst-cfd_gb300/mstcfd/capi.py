@@ -191,6 +191,8 @@ def load():
         "mst_mpnn_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
         "mst_mpnn_set_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
         "mst_mpnn_adam_step": (C.c_int, [C.c_void_p, C.c_float]),
+        "mst_mpnn_profile": (C.c_int, [C.c_void_p, C.c_int]),
+        "mst_mpnn_profile_read": (C.c_int, [C.c_void_p, _dp]),
         "mst_mesh3d_read_msh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
         "mst_mesh3d_get_info": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DInfo)]),
         "mst_mesh3d_get_arrays": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DArrays)]),

@@ -73,6 +73,19 @@ class Network:
     def adam_step(self, lr):
         capi.check(capi.load().mst_mpnn_adam_step(self._h, C.c_float(lr)))
 
+    def profile(self, on=True):
+        """Start (or stop) timing every tensor-core GEMM launch with CUDA
+        events; either clears what was recorded."""
+        capi.check(capi.load().mst_mpnn_profile(self._h, 1 if on else 0))
+
+    def profile_read(self):
+        """Summed GEMM time (ms), 2MNK flops, operand/result bytes and
+        launch count since the last profile()/profile_read(); clears them."""
+        out = np.zeros(4)
+        capi.check(capi.load().mst_mpnn_profile_read(self._h, out.ctypes.data_as(capi._dp)))
+        return {"ms": float(out[0]), "flops": float(out[1]), "bytes": float(out[2]),
+                "launches": int(out[3])}
+
     def close(self):
         h = getattr(self, "_h", None)
         if h:

@@ -117,8 +117,14 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
     phi = (double *)calloc((size_t)8 * (m->n_faces > 0 ? m->n_faces : 1), 8);
     pp.phi = phi;
   }
+  double l2_conv = 0.0;
   for (it = 0; it < niter; ++it) {
     double s = 0.0, l2;
+    if (converged) {
+      /* nothing of a converged case runs again: its state and norms stay */
+      if (l2_hist) l2_hist[it] = l2_conv;
+      continue;
+    }
     pp.phi_mode = phi ? frozen : 0;
     if (p->order == 2) om_gradient_ext(m, q, 0, grad);
     om_face_flux_ext(m, &pp, q, p->order == 2 ? grad : NULL, F);
@@ -140,8 +146,11 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
       if (first > 0.0 && l2 <= ip->freeze_tol * first && l2 > 0.7 * l2_win) frozen = 1;
       l2_win = l2;
     }
-    if (!converged && ip->tol > 0 && first > 0.0 && l2 <= ip->tol * first) converged = 1;
-    if (converged) continue; /* the state that met the tolerance is kept */
+    if (ip->tol > 0 && first > 0.0 && l2 <= ip->tol * first) {
+      converged = 1; /* the state that met the tolerance is kept */
+      l2_conv = l2;
+      continue;
+    }
     /* the CFL of this iteration from the norms of this residual */
     cfl = ip->cfl0;
     if (l2 > 0.0 && first > 0.0) cfl = ip->cfl0 * (first / l2);

@@ -21,7 +21,8 @@ typedef struct om_lusgs_params {
 
 /* niter LU-SGS iterations of one case in place (corrected-mode residual of
  * p, which must have quirks = 0); color [n_cells] the colour of each cell;
- * l2_hist [niter] (nullable) the L2 of R_rho / V before each update. */
+ * l2_hist [niter] (nullable) the L2 of R_rho / V before each update (after
+ * convergence nothing runs again and the converged L2 is repeated). */
 int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
                      const int *color, const om_lusgs_params *ip, int niter,
                      double *l2_hist);

@@ -115,3 +115,36 @@ def test_gpu_adam_training_lowers_the_loss():
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.2 * losses[0]
     net.close()
+
+
+@pytest.mark.gpu
+def test_gpu_gemm_profile_counts_the_launches():
+    """Live GEMM timing: a forward runs 5 tensor-core GEMMs (encoder, three
+    layers, decoder) whose 2MNK flops are known; a backward adds 9 (a weight
+    gradient and an input gradient per layer, the decoder's two, the
+    encoder's weight gradient)."""
+    from mstcfd.mpnn import Network
+    feats, ptr, nbr, targ = _graph(seed=4)
+    n = len(feats)
+    np_ = (n + 127) // 128 * 128
+    nk = (n + 63) // 64 * 64
+    net = Network(seed=1)
+    net.set_graph(feats, ptr, nbr)
+    net.set_targets(targ)
+    net.profile(True)
+    net.forward()
+    g = net.profile_read()
+    w, z, ink, out = 128, 256, 64, 4
+    assert g["launches"] == 5
+    assert g["flops"] == 2.0 * np_ * (w * ink + 3 * w * z + out * w)
+    assert g["ms"] > 0 and g["bytes"] > 0
+    net.backward()
+    g = net.profile_read()
+    assert g["launches"] == 9
+    wgrad = 2.0 * nk * (out * w + 3 * w * z + w * ink)
+    dgrad = 2.0 * np_ * (w * ink + 3 * z * w)
+    assert g["flops"] == wgrad + dgrad
+    net.profile(False)
+    net.forward()
+    assert net.profile_read()["launches"] == 0
+    net.close()
