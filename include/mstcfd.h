@@ -148,7 +148,8 @@ mst_status mst_mesh_get_arrays(const mst_mesh *m, mst_mesh_arrays *a);
  * zone header, each face line led by its node count).  Geometry by the
  * reference's 3D formulas (Face.cpp:20-39, Cell.cpp:6-14, :52-59; its cell
  * volume is the incomplete formula of the reference) plus the corrected
- * divergence-theorem volume.  Host only: no 3D residual kernels exist. */
+ * divergence-theorem volume.  mst_ctx3d_* below run the 3D residual path
+ * on them. */
 typedef struct mst_mesh3d mst_mesh3d;
 typedef struct mst_mesh3d_info {
   int n_nodes, n_cells, n_faces, n_int_faces, n_zones, n_face_nodes, n_cell_faces,
@@ -172,6 +173,69 @@ mst_status mst_mesh3d_get_info(const mst_mesh3d *m, mst_mesh3d_info *info);
 /* Copies out the arrays; every pointer may be NULL. */
 mst_status mst_mesh3d_get_arrays(const mst_mesh3d *m, mst_mesh3d_arrays *a);
 void mst_mesh3d_destroy(mst_mesh3d *m);
+/* A 3D mesh from arrays (generated meshes): face_ptr [nF+1] into
+ * face_nodes (3 or 4 nodes per face), face_cells [nF][2] (c1 = -1 on
+ * boundary faces), zones [n_zones][4] (id, first, last (1-based), Fluent
+ * type); c1_shift (nullable) [nF][3] = x(c0's frame) - x(c1's frame) of
+ * every face (non-zero on periodic faces, whose nodes are given in c0's
+ * frame).  Holds the arrays only: the reference-geometry arrays of
+ * mst_mesh3d_get_arrays stay empty for such a mesh. */
+mst_status mst_mesh3d_from_arrays(int n_nodes, const double *node_xyz, int n_cells, int n_faces,
+                                  const int *face_ptr, const int *face_nodes,
+                                  const int *face_cells, int n_zones, const int *zones,
+                                  const double *c1_shift, mst_mesh3d **out);
+
+/* ------------------------------------------------------------------ */
+/* 3D residual path                                                    */
+/* ------------------------------------------------------------------ */
+/* The reference's 3D path cannot run (2D-only thermodynamics,
+ * work/FUNCTION.cpp:3-18; wrong 3D volume and quad area, Cell.cpp:52-59,
+ * Face.cpp:30-36).  This is its 2D density path (RhoSolver.cpp:37-453, the
+ * corrected mode of mst_ctx) carried to 3D: corrected geometry (face
+ * centre = node mean, area 1/2 (n1-n0)x(n2-n0) or 1/2 (n2-n0)x(n3-n1),
+ * cell centre = mean of face centres, divergence-theorem volume), Green-
+ * Gauss gradient, split-axis Roe flux per axis (SolverRoe.cpp:70-123 with
+ * |A| dQ in closed form), unlimited or limited MUSCL, the laminar viscous
+ * term, BC zones as in 2D, explicit RK2 at a global CFL step.  States are
+ * [n_cells][5] (rho, rho u, rho v, rho w, E) in file order. */
+typedef struct mst_params3d {
+  int precision;     /* MST_PREC_* */
+  int order;         /* 1 or 2 */
+  int limiter;       /* MST_LIMITER_* (order 2) */
+  int viscous;       /* laminar viscous term (order 2) */
+  double mu, lambda, kappa, cv;
+  double inlet_q[5]; /* state of inlet faces */
+  double cfl;        /* CFL number of the global step */
+} mst_params3d;
+void mst_params3d_default(mst_params3d *p);
+typedef struct mst_ctx3d mst_ctx3d;
+typedef struct mst_ctx3d_info {
+  int n_cells, n_faces, n_tiles, max_tile_faces;
+  size_t device_bytes;
+} mst_ctx3d_info;
+mst_status mst_ctx3d_create(const mst_mesh3d *m, const mst_params3d *p, mst_ctx3d **out);
+mst_status mst_ctx3d_destroy(mst_ctx3d *c);
+mst_status mst_ctx3d_info_get(mst_ctx3d *c, mst_ctx3d_info *info);
+mst_status mst_ctx3d_set_state(mst_ctx3d *c, const double *q);
+mst_status mst_ctx3d_get_state(mst_ctx3d *c, double *q);
+/* residual R [n_cells][5] of the current state (sum over the cell's faces,
+ * ascending face id, of S_out . F); gradient [n_cells][3][5] */
+mst_status mst_ctx3d_residual(mst_ctx3d *c, double *r);
+mst_status mst_ctx3d_gradient(mst_ctx3d *c, double *g);
+/* nsteps RK2 steps at the global CFL step, the state kept in HBM; t_end >
+ * 0 cuts the last step to reach it.  Simulated time through *time
+ * (nullable).  mst_ctx3d_last_timing: device milliseconds and kernel
+ * launches of the last mst_ctx3d_step. */
+mst_status mst_ctx3d_step(mst_ctx3d *c, int nsteps, double t_end, double *time);
+mst_status mst_ctx3d_last_timing(mst_ctx3d *c, double *ms, int *launches);
+/* sum over cells of 1/2 |rho u|^2 / rho V, and of V */
+mst_status mst_ctx3d_kinetic_energy(mst_ctx3d *c, double *ke, double *vol);
+/* Per-kernel CUDA-event timing of mst_ctx3d_step launches (as
+ * mst_profile_*): on != 0 starts recording and clears the totals. */
+mst_status mst_ctx3d_profile(mst_ctx3d *c, int on);
+int mst_ctx3d_profile_count(mst_ctx3d *c);
+mst_status mst_ctx3d_profile_get(mst_ctx3d *c, int i, char *name, size_t name_len, int *launches,
+                                 double *total_ms);
 
 /* ------------------------------------------------------------------ */
 /* solver contexts: the RhoSolver surface                              */

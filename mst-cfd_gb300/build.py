@@ -13,6 +13,11 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/batch.cu          batched steady solves (LU-SGS orchestration,
                            CUDA graph, sweep autotuning)
   * csrc/mpnn.cu           the learned initial field (tcgen05 BF16 GEMMs)
+  * csrc/mesh3d.cpp        3D solver geometry and device layout (g++,
+                           -ffp-contract=off)
+  * csrc/kernels3d_exact.cu / kernels3d_fast.cu   3D residual kernels
+                           (FP64 parity without FMA; FP64 and FP32)
+  * csrc/solver3d.cu       the 3D path's C ABI (mst_ctx3d_*)
 """
 import os
 import shutil
@@ -57,6 +62,14 @@ def _units():
         ("io.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "io.cu")]),
         ("batch.o", [nv] + common + ["-c", os.path.join(CSRC, "batch.cu")]),
         ("mpnn.o", [nv] + common + ["-c", os.path.join(CSRC, "mpnn.cu")]),
+        ("mesh3d.o", ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                      "-Wall", "-c", os.path.join(CSRC, "mesh3d.cpp")]),
+        ("kernels3d_exact.o", [nv] + common + ["--fmad=false", "-c",
+                                               os.path.join(CSRC, "kernels3d_exact.cu")]),
+        ("kernels3d_fast.o", [nv] + common + ["-prec-div=false", "-prec-sqrt=false",
+                                              "-ftz=true", "-c",
+                                              os.path.join(CSRC, "kernels3d_fast.cu")]),
+        ("solver3d.o", [nv] + common + ["-c", os.path.join(CSRC, "solver3d.cu")]),
     ]
 
 

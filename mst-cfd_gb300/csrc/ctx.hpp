@@ -20,6 +20,10 @@ struct mst_mesh {
 
 struct mst_mesh3d {
   mst::HostMesh3D host;
+  // meshes from arrays: x(c0 frame) - x(c1 frame) per face ([nF][3]) or
+  // empty; from_arrays is true when the reference geometry was not built
+  std::vector<double> c1_shift;
+  bool from_arrays = false;
 };
 
 struct DevArrays {

@@ -57,6 +57,18 @@ class Mesh3DArrays(C.Structure):
                 ("cell_n_lower", _ip)]
 
 
+class Params3D(C.Structure):
+    _fields_ = [("precision", C.c_int), ("order", C.c_int), ("limiter", C.c_int),
+                ("viscous", C.c_int), ("mu", C.c_double), ("lambda_", C.c_double),
+                ("kappa", C.c_double), ("cv", C.c_double), ("inlet_q", C.c_double * 5),
+                ("cfl", C.c_double)]
+
+
+class Ctx3DInfo(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("n_tiles", C.c_int),
+                ("max_tile_faces", C.c_int), ("device_bytes", C.c_size_t)]
+
+
 class CaseParams(C.Structure):
     _fields_ = [("inlet_q", C.c_double * 4), ("mu", C.c_double), ("lambda_", C.c_double),
                 ("kappa", C.c_double), ("cv", C.c_double)]
@@ -197,6 +209,23 @@ def load():
         "mst_mesh3d_get_info": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DInfo)]),
         "mst_mesh3d_get_arrays": (C.c_int, [C.c_void_p, C.POINTER(Mesh3DArrays)]),
         "mst_mesh3d_destroy": (None, [C.c_void_p]),
+        "mst_mesh3d_from_arrays": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, _ip,
+                                             C.c_int, _ip, _dp, C.POINTER(C.c_void_p)]),
+        "mst_params3d_default": (None, [C.POINTER(Params3D)]),
+        "mst_ctx3d_create": (C.c_int, [C.c_void_p, C.POINTER(Params3D), C.POINTER(C.c_void_p)]),
+        "mst_ctx3d_destroy": (C.c_int, [C.c_void_p]),
+        "mst_ctx3d_info_get": (C.c_int, [C.c_void_p, C.POINTER(Ctx3DInfo)]),
+        "mst_ctx3d_set_state": (C.c_int, [C.c_void_p, _dp]),
+        "mst_ctx3d_get_state": (C.c_int, [C.c_void_p, _dp]),
+        "mst_ctx3d_residual": (C.c_int, [C.c_void_p, _dp]),
+        "mst_ctx3d_gradient": (C.c_int, [C.c_void_p, _dp]),
+        "mst_ctx3d_step": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp]),
+        "mst_ctx3d_last_timing": (C.c_int, [C.c_void_p, _dp, _ip]),
+        "mst_ctx3d_kinetic_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "mst_ctx3d_profile": (C.c_int, [C.c_void_p, C.c_int]),
+        "mst_ctx3d_profile_count": (C.c_int, [C.c_void_p]),
+        "mst_ctx3d_profile_get": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t, _ip,
+                                            _dp]),
         "mst_lu_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _dp,
                                     C.POINTER(C.c_void_p)]),
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),

@@ -1,5 +1,6 @@
-"""3D Fluent meshes (mst_mesh3d_* of the C ABI): the reader of
-MshBlock::readMsh with DIM 3 and its geometry, host only."""
+"""3D meshes (mst_mesh3d_* of the C ABI): the reader of MshBlock::readMsh
+with DIM 3 and its reference geometry, or a mesh from arrays (generated,
+optionally periodic); mstcfd.solver3d runs the 3D residual path on both."""
 import ctypes as C
 import os
 
@@ -9,14 +10,46 @@ from . import capi
 
 
 class Mesh3D:
-    def __init__(self, path):
-        h = C.c_void_p()
-        capi.check(capi.load().mst_mesh3d_read_msh(os.fsencode(path), C.byref(h)))
+    def __init__(self, path=None, _handle=None):
+        h = _handle
+        if h is None:
+            h = C.c_void_p()
+            capi.check(capi.load().mst_mesh3d_read_msh(os.fsencode(path), C.byref(h)))
         self._h = h
         i = capi.Mesh3DInfo()
         capi.check(capi.load().mst_mesh3d_get_info(self._h, C.byref(i)))
         self.info = {k: getattr(i, k) for k, _ in capi.Mesh3DInfo._fields_}
         self.n_cells, self.n_faces = i.n_cells, i.n_faces
+
+    @classmethod
+    def from_arrays(cls, node_xyz, faces, face_cells, zones, n_cells, c1_shift=None):
+        """faces: [nF][3 or 4] array or a list of node lists (c0's frame for
+        periodic faces); zones [nz][4] (id, first, last, type); c1_shift
+        [nF][3] x(c0 frame) - x(c1 frame) or None."""
+        if isinstance(faces, np.ndarray):
+            ptr = np.arange(0, faces.size + 1, faces.shape[1], dtype=np.int32)
+            fn = np.ascontiguousarray(faces.ravel(), np.int32)
+        else:
+            ptr = np.zeros(len(faces) + 1, np.int32)
+            ptr[1:] = np.cumsum([len(f) for f in faces])
+            fn = np.array([v for f in faces for v in f], np.int32)
+        xyz = np.ascontiguousarray(node_xyz, np.float64)
+        fc = np.ascontiguousarray(face_cells, np.int32)
+        zn = np.ascontiguousarray(zones, np.int32).reshape(-1, 4)
+        sh = None if c1_shift is None else np.ascontiguousarray(c1_shift, np.float64)
+        h = C.c_void_p()
+        capi.check(capi.load().mst_mesh3d_from_arrays(
+            len(xyz), xyz.ctypes.data_as(capi._dp), int(n_cells), len(ptr) - 1,
+            ptr.ctypes.data_as(capi._ip), fn.ctypes.data_as(capi._ip),
+            fc.ctypes.data_as(capi._ip), len(zn), zn.ctypes.data_as(capi._ip),
+            sh.ctypes.data_as(capi._dp) if sh is not None else None, C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
+    def from_dict(cls, m):
+        """From a meshgen 3D mesh dict."""
+        return cls.from_arrays(m["node_xyz"], m["faces"], m["face_cells"], m["zones"],
+                               m["n_cells"], m.get("c1_shift"))
 
     def arrays(self):
         i = self.info

@@ -459,6 +459,107 @@ def hex_box(n=4, length=1.0, jitter=0.0, seed=1,
     return _assemble3d(xyz, cells, len(cells), side_of, kinds)
 
 
+def tet_grid(n, length=2 * np.pi, jitter=0.15, seed=20261205):
+    """Periodic [0, L)^3: an n^3 lattice of hexahedra, each split into 6
+    tetrahedra along its main diagonal (the Kuhn subdivision, conforming
+    across hexahedra), nodes moved by U(-jitter h, +jitter h) per axis.
+    6 n^3 cells, 12 n^3 triangular faces, all interior.  Vectorised (no
+    Python loop over cells) for the 128^3 x 6 = 12.6M-cell workload.
+
+    Nodes are the (n+1)^3 unwrapped lattice points (the images at index n
+    carry the jitter of index 0 plus L); every face lists its nodes in the
+    frame of its c0 and carries c1_shift = x(c0 frame) - x(c1 frame), a
+    multiple of L per axis.  Every area vector points into c0."""
+    n = int(n)
+    if n < 2 or n > 128:
+        raise ValueError("tet_grid: 2 <= n <= 128")
+    h = length / n
+    n1 = n + 1
+    rng = np.random.default_rng(seed)
+    jit = rng.uniform(-jitter, jitter, (n ** 3, 3))
+    g = np.stack(np.meshgrid(np.arange(n1), np.arange(n1), np.arange(n1), indexing="ij"),
+                 -1).reshape(-1, 3)
+    wrap = ((g[:, 0] % n) * n + (g[:, 1] % n)) * n + (g[:, 2] % n)
+    xyz = (g + jit[wrap]) * h
+    # rows: (cube, tet, face) -> the face's 3 cube corners
+    corner = np.array([[c & 1, (c >> 1) & 1, (c >> 2) & 1] for c in range(8)], np.int64)
+    tri = []
+    for t in _KUHN:
+        tri += [[t[0], t[1], t[2]], [t[0], t[1], t[3]], [t[0], t[2], t[3]], [t[1], t[2], t[3]]]
+    tri = np.array(tri, np.int64)                       # [24][3] corners
+    cube = np.arange(n ** 3, dtype=np.int64)
+    base = np.stack([cube // (n * n), (cube // n) % n, cube % n], 1)  # [n^3][3]
+    # lattice coordinates of every row's 3 nodes: [n^3, 24, 3(node), 3(axis)]
+    lat = base[:, None, None, :] + corner[tri][None, :, :, :]
+    lat = lat.reshape(-1, 3, 3)
+    uid = (lat[..., 0] * n1 + lat[..., 1]) * n1 + lat[..., 2]          # unwrapped ids
+    wid = ((lat[..., 0] % n) * n + lat[..., 1] % n) * n + lat[..., 2] % n
+    del lat
+    cell = np.repeat(np.arange(6 * n ** 3, dtype=np.int64), 4)
+    ws = np.sort(wid, 1)
+    key = (ws[:, 0] << 42) | (ws[:, 1] << 21) | ws[:, 2]
+    del ws
+    order = np.argsort(key, kind="stable")
+    a, b = order[0::2], order[1::2]
+    if not np.array_equal(key[a], key[b]):
+        raise RuntimeError("tet_grid: unpaired face")
+    del key, order
+    # faces in c0 order (the row of the lower cell comes first)
+    f0 = np.minimum(a, b)
+    f1 = np.maximum(a, b)
+    o = np.argsort(f0, kind="stable")
+    f0, f1 = f0[o], f1[o]
+    c0, c1 = cell[f0], cell[f1]
+    nodes = uid[f0]                                       # c0's frame
+    # c1_shift: the same wrapped node in both rows
+    w0 = wid[f0, 0]
+    hit = (wid[f1] == w0[:, None])
+    j1 = np.argmax(hit, 1)
+    u1 = uid[f1, j1]
+    l0 = np.stack([nodes[:, 0] // (n1 * n1), (nodes[:, 0] // n1) % n1, nodes[:, 0] % n1], 1)
+    l1 = np.stack([u1 // (n1 * n1), (u1 // n1) % n1, u1 % n1], 1)
+    shift = ((l0 - l1) // n).astype(np.float64) * length
+    # orientation: the area vector (n1-n0) x (n2-n0) points into c0
+    p0, p1, p2 = xyz[nodes[:, 0]], xyz[nodes[:, 1]], xyz[nodes[:, 2]]
+    nrm = np.cross(p1 - p0, p2 - p0)
+    fc = (p0 + p1 + p2) / 3.0
+    cubes0 = c0 // 6
+    t0 = c0 % 6
+    kuhn = np.array(_KUHN, np.int64)
+    cc = (base[cubes0][:, None, :] + corner[kuhn[t0]]).astype(np.float64)  # lattice corners
+    cen = ((cc + jit[(((cc[..., 0] % n) * n + cc[..., 1] % n) * n + cc[..., 2] % n)
+                     .astype(np.int64)]) * h).mean(1)
+    flip = np.einsum("ij,ij->i", nrm, fc - cen) > 0
+    nodes[flip, 1], nodes[flip, 2] = nodes[flip, 2].copy(), nodes[flip, 1].copy()
+    nF = len(nodes)
+    # cell centroids (mean of the 4 nodes, own frame)
+    allc = np.arange(6 * n ** 3, dtype=np.int64)
+    ccl = (base[allc // 6][:, None, :] + corner[kuhn[allc % 6]]).astype(np.int64)
+    cwr = ((ccl[..., 0] % n) * n + ccl[..., 1] % n) * n + ccl[..., 2] % n
+    centroid = ((ccl + jit[cwr]) * h).mean(1)
+    return {"node_xyz": xyz, "faces": nodes.astype(np.int32),
+            "face_cells": np.stack([c0, c1], 1).astype(np.int32),
+            "zones": np.array([[3, 1, nF, INTERIOR]], np.int32), "n_cells": 6 * n ** 3,
+            "c1_shift": shift, "cell_centroid": centroid}
+
+
+def taylor_green(xyz, mach=0.1, rho0=1.0, length=2 * np.pi):
+    """Compressible Taylor-Green vortex on [0, 2 pi)^3 (L = 1 per radian):
+    u = V0 sin x cos y cos z, v = -V0 cos x sin y cos z, w = 0,
+    p = p0 + rho0 V0^2 / 16 (cos 2x + cos 2y)(cos 2z + 2), rho = rho0 p/p0
+    (isothermal start), V0 = mach (speed of sound 1: p0 = rho0 / gamma)."""
+    x, y, z = (xyz[:, k] * (2 * np.pi / length) for k in range(3))
+    v0 = mach
+    p0 = rho0 / GAMMA
+    u = v0 * np.sin(x) * np.cos(y) * np.cos(z)
+    v = -v0 * np.cos(x) * np.sin(y) * np.cos(z)
+    w = np.zeros_like(u)
+    p = p0 + rho0 * v0 ** 2 / 16.0 * (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0)
+    rho = rho0 * p / p0
+    E = p / (GAMMA - 1.0) + 0.5 * rho * (u * u + v * v + w * w)
+    return np.stack([rho, rho * u, rho * v, rho * w, E], 1)
+
+
 def write_msh3d(path, mesh, mixed_zones=(), crlf=False):
     """Fluent ASCII 3D .msh: zones with a fixed face node count, or, for the
     zone indices in mixed_zones, a mixed zone (node count 0 in the header,

@@ -16,7 +16,7 @@ REF_OUT = os.path.join(HERE, "_ref")
 REF_SRC = os.environ.get("MSTCFD_REF_SRC", "/root/reference/MST-CFD")
 
 _SOURCES = ["mstoracle.c", "mstoracle_ext.c", "mstoracle_lu.c", "mstoracle_io.c",
-            "mstoracle_implicit.c"]
+            "mstoracle_implicit.c", "mstoracle3d.c"]
 
 
 def _stale(target, deps):
@@ -29,7 +29,8 @@ def _stale(target, deps):
 def build_oracle(force=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(HERE, s) for s in _SOURCES if os.path.exists(os.path.join(HERE, s))]
-    deps = srcs + [os.path.join(HERE, "mstoracle.h")]
+    deps = srcs + [os.path.join(HERE, h) for h in
+                   ("mstoracle.h", "mstoracle_io.h", "mstoracle_implicit.h", "mstoracle3d.h")]
     if force or _stale(LIB, deps):
         cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
                "-ffp-contract=off", "-Wall", "-o", LIB] + srcs + ["-lm"]

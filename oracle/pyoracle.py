@@ -386,3 +386,170 @@ def lusgs_iterate(mesh, prm, q, color, niter, cfl0=5.0, cfl_max=200.0, omega=1.5
     if rc != 0:
         raise ValueError(f"oracle: lusgs failed (status {rc})")
     return q, hist[:int(niter)]
+
+
+# ---------------------------------------------------------------------------
+# 3D path (mstoracle3d.c): states [n_cells, 5], gradients [n_cells, 3, 5],
+# face fluxes [n_faces, 3, 5]
+# ---------------------------------------------------------------------------
+class _O3Input(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_cells", C.c_int), ("n_faces", C.c_int),
+                ("node_xyz", _dp), ("face_ptr", _ip), ("face_nodes", _ip),
+                ("face_cells", _ip), ("face_type", _ip), ("c1_shift", _dp)]
+
+
+class _O3Mesh(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("face_cells", _ip),
+                ("face_kind", _ip), ("face_ctr", _dp), ("face_dir", _dp), ("r0", _dp),
+                ("r1", _dp), ("eta", _dp), ("cell_ctr", _dp), ("cell_vol", _dp),
+                ("cell_ptr", _ip), ("cell_faces", _ip), ("cell_nb", _ip), ("cell_dir", _dp),
+                ("cell_w", _dp)]
+
+
+class _O3Params(C.Structure):
+    _fields_ = [("order", C.c_int), ("limiter", C.c_int), ("viscous", C.c_int),
+                ("mu", C.c_double), ("lam", C.c_double), ("kappa", C.c_double),
+                ("cv", C.c_double), ("inlet", C.c_double * 5)]
+
+
+_lib3 = None
+
+
+def lib3():
+    global _lib3
+    if _lib3 is None:
+        L = lib()
+        M = C.POINTER(_O3Mesh)
+        L.om3_build.argtypes = [C.POINTER(_O3Input), M]
+        L.om3_free.argtypes = [M]
+        L.om3_gradient.argtypes = [M, _dp, _dp]
+        L.om3_face_flux.argtypes = [M, C.POINTER(_O3Params), _dp, _dp, _dp]
+        L.om3_gather.argtypes = [M, _dp, _dp]
+        L.om3_residual.argtypes = [M, C.POINTER(_O3Params), _dp, _dp]
+        L.om3_dt.argtypes = [M, _dp, C.c_double]
+        L.om3_dt.restype = C.c_double
+        L.om3_rk2.argtypes = [M, C.POINTER(_O3Params), _dp, C.c_int, C.c_double, C.c_double,
+                              _dp]
+        L.om3_kinetic_energy.argtypes = [M, _dp, _dp, _dp]
+        _lib3 = L
+    return _lib3
+
+
+def _zone_types(zones, n_faces):
+    t = np.zeros(n_faces, np.int32)
+    for _, first, last, ty in np.asarray(zones).reshape(-1, 4).tolist():
+        t[first - 1:last] = ty
+    return t
+
+
+class Mesh3:
+    """Oracle 3D mesh: the solver geometry of mstoracle3d.c (file numbering)."""
+
+    def __init__(self, node_xyz, faces, face_cells, zones, n_cells, c1_shift=None):
+        faces = [list(f) for f in faces] if not isinstance(faces, np.ndarray) else faces
+        if isinstance(faces, np.ndarray):
+            ptr = np.arange(0, faces.size + 1, faces.shape[1], dtype=np.int32)
+            fn = np.ascontiguousarray(faces.ravel(), np.int32)
+        else:
+            ptr = np.zeros(len(faces) + 1, np.int32)
+            ptr[1:] = np.cumsum([len(f) for f in faces])
+            fn = np.array([v for f in faces for v in f], np.int32)
+        self._keep = [_f64(node_xyz), ptr, fn, np.ascontiguousarray(face_cells, np.int32),
+                      _zone_types(zones, len(ptr) - 1)]
+        shift = None if c1_shift is None else _f64(c1_shift)
+        self._keep.append(shift)
+        xyz, ptr, fn, fc, ft = self._keep[:5]
+        inp = _O3Input(len(xyz), int(n_cells), len(ptr) - 1, _d(xyz), _i(ptr), _i(fn), _i(fc),
+                       _i(ft), _d(shift) if shift is not None else None)
+        self._m = _O3Mesh()
+        if lib3().om3_build(C.byref(inp), C.byref(self._m)) != 0:
+            raise ValueError("oracle: bad 3D mesh")
+        self.n_cells = int(n_cells)
+        self.n_faces = len(ptr) - 1
+
+    def _arr(self, name, n, dt=np.float64):
+        p = getattr(self._m, name)
+        return np.ctypeslib.as_array(p, shape=(n,)).astype(dt).copy()
+
+    def arrays(self):
+        nF, nC = self.n_faces, self.n_cells
+        tot = int(self._arr("cell_ptr", nC + 1, np.int64)[-1])
+        return {"face_ctr": self._arr("face_ctr", 3 * nF).reshape(nF, 3),
+                "face_dir": self._arr("face_dir", 3 * nF).reshape(nF, 3),
+                "r0": self._arr("r0", 3 * nF).reshape(nF, 3),
+                "r1": self._arr("r1", 3 * nF).reshape(nF, 3),
+                "eta": self._arr("eta", nF),
+                "face_kind": self._arr("face_kind", nF, np.int32),
+                "cell_ctr": self._arr("cell_ctr", 3 * nC).reshape(nC, 3),
+                "cell_vol": self._arr("cell_vol", nC),
+                "cell_ptr": self._arr("cell_ptr", nC + 1, np.int32),
+                "cell_faces": self._arr("cell_faces", tot, np.int32),
+                "cell_nb": self._arr("cell_nb", tot, np.int32),
+                "cell_dir": self._arr("cell_dir", 3 * tot).reshape(tot, 3)}
+
+    def __del__(self):
+        try:
+            if getattr(self, "_m", None) is not None and _lib3 is not None:
+                _lib3.om3_free(C.byref(self._m))
+                self._m = None
+        except Exception:
+            pass
+
+
+def params3(order=2, limiter=3, viscous=0, mu=0.0, lam=0.0, kappa=0.0, cv=1.0, inlet=None):
+    p = _O3Params(int(order), int(limiter), int(viscous), float(mu), float(lam), float(kappa),
+                  float(cv))
+    if inlet is not None:
+        for k in range(5):
+            p.inlet[k] = float(inlet[k])
+    return p
+
+
+def gradient3(mesh, q):
+    q = _f64(q)
+    g = np.zeros((mesh.n_cells, 3, 5))
+    lib3().om3_gradient(C.byref(mesh._m), _d(q), _d(g))
+    return g
+
+
+def face_flux3(mesh, prm, q, grad=None):
+    q = _f64(q)
+    F = np.zeros((mesh.n_faces, 3, 5))
+    g = None if grad is None else _f64(grad)
+    lib3().om3_face_flux(C.byref(mesh._m), C.byref(prm), _d(q), _d(g) if g is not None else None,
+                         _d(F))
+    return F
+
+
+def gather3(mesh, F):
+    F = _f64(F)
+    R = np.zeros((mesh.n_cells, 5))
+    lib3().om3_gather(C.byref(mesh._m), _d(F), _d(R))
+    return R
+
+
+def residual3(mesh, prm, q):
+    q = _f64(q)
+    R = np.zeros((mesh.n_cells, 5))
+    lib3().om3_residual(C.byref(mesh._m), C.byref(prm), _d(q), _d(R))
+    return R
+
+
+def dt3(mesh, q, cfl):
+    return float(lib3().om3_dt(C.byref(mesh._m), _d(_f64(q)), float(cfl)))
+
+
+def rk2_3(mesh, prm, q, nsteps, cfl, t_end=0.0, time=0.0):
+    """nsteps RK2 steps; returns (q, time)."""
+    q = _f64(q).copy()
+    t = C.c_double(time)
+    if lib3().om3_rk2(C.byref(mesh._m), C.byref(prm), _d(q), int(nsteps), float(cfl),
+                      float(t_end), C.byref(t)) != 0:
+        raise ValueError("oracle: rk2 failed")
+    return q, t.value
+
+
+def kinetic_energy3(mesh, q):
+    ke, v = C.c_double(), C.c_double()
+    lib3().om3_kinetic_energy(C.byref(mesh._m), _d(_f64(q)), C.byref(ke), C.byref(v))
+    return ke.value, v.value

@@ -1,0 +1,247 @@
+"""The 3D residual path (mst_ctx3d_*; the 2D density path's corrected mode
+carried to 3D, checked against its CPU restatement oracle/mstoracle3d.c).
+
+CPU: the periodic Kuhn tetrahedral generator (closure, volumes, centroids),
+the restatement's free-stream preservation and discrete conservation, the
+from-arrays mesh handle.
+GPU: the FP64 exact path is bit-identical to the restatement (gradient,
+residual with every order / limiter / the viscous term, on a periodic
+mesh and on a box with inlet, outlet, wall and symmetry zones; RK2 steps
+with the global CFL step); FP64 with FMA within 1e-12 and the FP32 path
+within FP32 rounding of it; FP32 conserves mass to float-pair accuracy;
+the viscous term decays a shear wave at the analytic rate; the Taylor-Green
+kinetic energy decays, FP32 tracking FP64.
+"""
+import numpy as np
+import pytest
+
+GAMMA = 1.4
+CV = 1.0 / (GAMMA * (GAMMA - 1.0))
+
+
+def _tgv_mesh(n=4, jitter=0.15, seed=3):
+    from mstcfd import meshgen as mg
+    return mg.tet_grid(n, jitter=jitter, seed=seed)
+
+
+def _oracle(m):
+    from oracle import pyoracle as po
+    return po.Mesh3(m["node_xyz"], m["faces"], m["face_cells"], m["zones"], m["n_cells"],
+                    m.get("c1_shift"))
+
+
+def _visc(mu=0.1 / 1600):
+    return dict(mu=mu, lam=-2.0 / 3.0 * mu, kappa=mu * GAMMA * CV / 0.71, cv=CV)
+
+
+def test_tet_grid_geometry():
+    m = _tgv_mesh(5)
+    A = _oracle(m).arrays()
+    assert m["n_cells"] == 6 * 125 and len(m["faces"]) == 12 * 125
+    assert np.isclose(A["cell_vol"].sum(), (2 * np.pi) ** 3, rtol=1e-13)
+    assert A["cell_vol"].min() > 0
+    assert np.abs(A["cell_ctr"] - m["cell_centroid"]).max() < 1e-13
+    ptr = A["cell_ptr"]
+    assert np.all(np.diff(ptr) == 4)
+    closure = np.add.reduceat(A["cell_dir"], ptr[:-1], axis=0)
+    assert np.abs(closure).max() < 1e-13
+    # periodic shifts are whole periods
+    s = m["c1_shift"] / (2 * np.pi)
+    assert np.allclose(s, np.round(s)) and np.abs(s).max() == 1.0
+
+
+def test_oracle3d_freestream_and_conservation():
+    from mstcfd import meshgen as mg
+    from oracle import pyoracle as po
+    m = _tgv_mesh(4)
+    om = _oracle(m)
+    q = np.array([1.0, 0.3, 0.2, -0.1, 1 / (GAMMA * 0.4) + 0.5 * 0.14])
+    Q = np.tile(q, (m["n_cells"], 1))
+    for order, lim, visc in ((1, 0, 0), (2, 0, 0), (2, 3, 0), (2, 1, 1)):
+        p = po.params3(order=order, limiter=lim, viscous=visc, **_visc())
+        assert np.abs(po.residual3(om, p, Q)).max() < 1e-13
+    q0 = mg.taylor_green(m["cell_centroid"])
+    R = po.residual3(om, po.params3(order=2, limiter=3, viscous=1, **_visc()), q0)
+    assert np.abs(R).max() > 1e-3
+    assert np.abs(R.sum(0)).max() < 1e-14 * np.abs(R).sum()
+
+
+def test_mesh3d_from_arrays_handle():
+    from mstcfd.mesh3d import Mesh3D
+    m = _tgv_mesh(3)
+    h = Mesh3D.from_dict(m)
+    a = h.arrays()
+    assert h.n_cells == m["n_cells"] and h.n_faces == len(m["faces"])
+    assert np.array_equal(a["face_nodes"].reshape(-1, 3), m["faces"])
+    assert np.array_equal(a["face_cells"], m["face_cells"])
+    h.close()
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def _box():
+    from mstcfd import meshgen as mg
+    # inlet x-, outlet x+, walls y-/y+, symmetry z-/z+
+    return mg.tet_box(3, length=1.0, jitter=0.15, seed=5)
+
+
+def _box_state(m, rng):
+    n = int(m["n_cells"])
+    rho = 1.0 + 0.1 * rng.standard_normal(n)
+    u = 0.5 + 0.1 * rng.standard_normal(n)
+    v = 0.1 * rng.standard_normal(n)
+    w = 0.1 * rng.standard_normal(n)
+    p = 1 / GAMMA + 0.05 * rng.standard_normal(n)
+    return np.stack([rho, rho * u, rho * v, rho * w,
+                     p / 0.4 + 0.5 * rho * (u * u + v * v + w * w)], 1)
+
+
+def _solver(m, **kw):
+    from mstcfd.mesh3d import Mesh3D
+    from mstcfd.solver3d import Solver3D
+    return Solver3D(Mesh3D.from_dict(m), **kw)
+
+
+CASES = [(1, 0, 0), (2, 0, 0), (2, 1, 0), (2, 2, 0), (2, 3, 0), (2, 3, 1)]
+INLET = [1.0, 0.5, 0.0, 0.0, 1 / (GAMMA * 0.4) + 0.125]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mesh", ["periodic", "box"])
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"o{c[0]}l{c[1]}v{c[2]}")
+def test_gpu3d_exact_residual_matches_oracle(mesh, case):
+    from mstcfd import meshgen as mg
+    from oracle import pyoracle as po
+    order, lim, visc = case
+    if mesh == "periodic":
+        m = _tgv_mesh(4)
+        q = mg.taylor_green(m["cell_centroid"], mach=0.3)
+    else:
+        m = _box()
+        q = _box_state(m, np.random.default_rng(1))
+    om = _oracle(m)
+    kw = _visc(1e-2)
+    s = _solver(m, precision=0, order=order, limiter=lim, viscous=visc, mu=kw["mu"],
+                lambda_=kw["lam"], kappa=kw["kappa"], cv=kw["cv"], inlet_q=INLET)
+    s.set_state(q)
+    assert np.array_equal(s.state(), q)
+    p = po.params3(order=order, limiter=lim, viscous=visc, inlet=INLET, **kw)
+    R = po.residual3(om, p, q)
+    assert np.array_equal(s.residual(), R)
+    if order == 2:
+        assert np.array_equal(s.gradient(), po.gradient3(om, q))
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("visc", [0, 1])
+def test_gpu3d_exact_rk2_matches_oracle(visc):
+    from mstcfd import meshgen as mg
+    from oracle import pyoracle as po
+    m = _tgv_mesh(4)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.3)
+    om = _oracle(m)
+    kw = _visc(1e-2)
+    s = _solver(m, precision=0, order=2, limiter=3, viscous=visc, mu=kw["mu"], lambda_=kw["lam"],
+                kappa=kw["kappa"], cv=kw["cv"], cfl=0.5)
+    s.set_state(q0)
+    t = s.step(4)
+    q, tq = po.rk2_3(om, po.params3(order=2, limiter=3, viscous=visc, **kw), q0, 4, 0.5)
+    assert t == tq
+    assert np.array_equal(s.state(), q)
+    # the last step is cut to reach t_end exactly
+    t2 = s.step(10, t_end=t + 0.05)
+    q2, tq2 = po.rk2_3(om, po.params3(order=2, limiter=3, viscous=visc, **kw), q, 10, 0.5,
+                       t_end=tq + 0.05, time=tq)
+    assert t2 == tq2 and np.array_equal(s.state(), q2)
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [(1, 1e-12), (2, 2e-5)], ids=["fp64", "fp32"])
+def test_gpu3d_production_precisions_track_exact(prec, tol):
+    from mstcfd import meshgen as mg
+    m = _tgv_mesh(6)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.3)
+    kw = _visc(1e-2)
+    out = {}
+    for p in (0, prec):
+        s = _solver(m, precision=p, order=2, limiter=3, viscous=1, mu=kw["mu"], lambda_=kw["lam"],
+                    kappa=kw["kappa"], cv=kw["cv"])
+        s.set_state(q0)
+        r = s.residual()
+        s.step(5)
+        out[p] = (r, s.state())
+        s.close()
+    r0, q0e = out[0]
+    r1, q1 = out[prec]
+    assert np.abs(r1 - r0).max() <= tol * 50 * np.abs(r0).max()
+    assert np.abs(q1 - q0e).max() <= tol * np.abs(q0e).max()
+
+
+@pytest.mark.gpu
+def test_gpu3d_fp32_conserves_mass():
+    from mstcfd import meshgen as mg
+    m = _tgv_mesh(8)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.3)
+    vol = _oracle(m).arrays()["cell_vol"]
+    s = _solver(m, precision=2, order=2, limiter=3, viscous=1, mu=1e-3, lambda_=-2e-3 / 3,
+                kappa=1e-3 * GAMMA * CV / 0.71, cv=CV)
+    s.set_state(q0)
+    s.step(20)
+    q = s.state()
+    m0, m1 = (q0[:, 0] * vol).sum(), (q[:, 0] * vol).sum()
+    assert abs(m1 - m0) <= 1e-12 * m0
+    s.close()
+
+
+@pytest.mark.gpu
+def test_gpu3d_shear_wave_viscous_decay():
+    """u = U sin(y) (y in radians), periodic: kinetic energy decays as
+    exp(-2 nu t) (k = 1); the inviscid run keeps it to within its numerical
+    dissipation, so the viscous decay is taken relative to it."""
+    from mstcfd import meshgen as mg
+    m = _tgv_mesh(16, jitter=0.1)
+    xyz = m["cell_centroid"]
+    U, nu = 0.05, 0.02
+    rho = np.ones(len(xyz))
+    u = U * np.sin(xyz[:, 1])
+    p = np.full(len(xyz), 1 / GAMMA)
+    q0 = np.stack([rho, rho * u, 0 * u, 0 * u, p / 0.4 + 0.5 * rho * u * u], 1)
+    ke = {}
+    for visc in (0, 1):
+        s = _solver(m, precision=1, order=2, limiter=0, viscous=visc, mu=nu, lambda_=-2 * nu / 3,
+                    kappa=0.0, cv=CV, cfl=0.5)
+        s.set_state(q0)
+        k0, _ = s.kinetic_energy()
+        t = s.step(2000, t_end=2.0)
+        k1, _ = s.kinetic_energy()
+        ke[visc] = (k0, k1, t)
+        s.close()
+    assert ke[0][2] == 2.0 and ke[1][2] == 2.0
+    ratio = (ke[1][1] / ke[1][0]) / (ke[0][1] / ke[0][0])
+    # within 5% of the analytic decay (Green-Gauss gradients on h = 0.39)
+    assert abs(ratio - np.exp(-2 * nu * 2.0)) < 0.05 * (1 - np.exp(-2 * nu * 2.0))
+
+
+@pytest.mark.gpu
+def test_gpu3d_tgv_kinetic_energy_decays_fp32_tracks_fp64():
+    from mstcfd import meshgen as mg
+    m = _tgv_mesh(12)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.1)
+    kw = _visc()
+    hist = {}
+    for prec in (1, 2):
+        s = _solver(m, precision=prec, order=2, limiter=3, viscous=1, mu=kw["mu"],
+                    lambda_=kw["lam"], kappa=kw["kappa"], cv=kw["cv"], cfl=0.5)
+        s.set_state(q0)
+        h = [s.kinetic_energy()[0]]
+        for _ in range(4):
+            s.step(1000, t_end=0.25 * (len(h)))
+            h.append(s.kinetic_energy()[0])
+        hist[prec] = np.array(h)
+        s.close()
+    for h in hist.values():
+        assert np.all(np.diff(h) < 0)
+    assert np.abs(hist[2] - hist[1]).max() <= 1e-4 * hist[1][0]
