@@ -488,6 +488,97 @@ def run_cpu_sample(m, steps, budget_s=30.0):
     return 2.0 * m["n_cells"] * done / t_total / 1e6, cores, done, t_total
 
 
+def run_tgv3d(args, grp):
+    """3D Taylor-Green vortex (Ma 0.1, Re 1600, laminar) on the periodic
+    jittered Kuhn tetrahedral mesh of (tgv_n)^3 x 6 cells: FP32 and FP64
+    Mcell-updates/s of RK2 steps (Roe + van Albada + viscous term, CFL 0.5),
+    the dominant kernel against the HBM roofline, and the CPU restatement
+    timed on a bounded sample of the same family."""
+    from mstcfd import meshgen as mg
+    from mstcfd import roofline as rl
+    from mstcfd.mesh3d import Mesh3D
+    from mstcfd.solver3d import Solver3D
+    n = args.tgv_n
+    t0 = time.perf_counter()
+    m = mg.tet_grid(n, jitter=0.15, seed=20261205)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.1)
+    mesh = Mesh3D.from_dict(m)
+    setup_s = time.perf_counter() - t0
+    nC = int(m["n_cells"])
+    mu = 0.1 / 1600.0  # rho V0 L / mu = 1600 with V0 = Ma 0.1 x a (= 1), L = 1
+    cv = 1.0 / (1.4 * 0.4)
+    kw = dict(order=2, limiter=3, viscous=1, mu=mu, lambda_=-2.0 / 3.0 * mu,
+              kappa=mu * 1.4 * cv / 0.71, cv=cv, cfl=0.5)
+    hbm, src = _peaks()
+    out = {"workload": f"3D Taylor-Green vortex, Ma 0.1, Re 1600, periodic [0,2pi)^3, "
+                       f"{n}^3 hexahedra x 6 jittered tetrahedra ({nC} cells), Roe + van "
+                       f"Albada + laminar viscous term, RK2, CFL 0.5",
+           "cells": nC, "faces": len(m["faces"]), "mesh_setup_s": round(setup_s, 1),
+           "step": "one RK2 time step = 2 cell-updates per cell",
+           "l2": "inputs larger than L2 (state + mesh ~10 GB)"}
+    for prec, label in ((2, "fp32"), (1, "fp64")):
+        s = Solver3D(mesh, precision=prec, **kw)
+        info = s.info
+        s.set_state(q0)
+        ke0 = s.kinetic_energy()[0]
+        s.step(max(3, args.warmup))
+        steps = args.tgv_steps if prec == 2 else max(2, args.tgv_steps // 5)
+        grp.barrier()
+        s.step(steps)
+        ms, launches = s.last_timing()
+        ms = grp.max(ms)
+        s.profile(True)
+        s.step(steps)
+        prof = s.profile_stats()
+        s.profile(False)
+        ke1 = s.kinetic_energy()[0]
+        t = s.step(0)
+        res = {"value": round(2 * nC * steps * grp.ws / (ms * 1e-3) / 1e6, 2),
+               "unit": UNIT, "ms_per_step": round(ms / steps, 4), "steps": steps,
+               "gpu_launches": launches, "device_gb": round(info["device_bytes"] / 1e9, 2),
+               "kinetic_energy": {"t0": ke0, "t": t, "ratio": ke1 / ke0}}
+        if "k3_flux_update" in prof:
+            nl, tot_ms = prof["k3_flux_update"]
+            by = 0.5 * sum(rl.kernel_bytes3d(nC, info["n_faces"], info["n_cell_faces"],
+                                             info["n_tiles"], info["n_borrowed"], prec, 2, 1,
+                                             "k3_flux_update", stage=st) for st in (0, 1))
+            avg = tot_ms / nl
+            res["roofline"] = {"bound": "hbm", "kernel": "k3_flux_update",
+                               "achieved": round(by / (avg * 1e-3) / 1e9, 1), "peak": hbm,
+                               "unit": "GB/s", "frac": round(by / (avg * 1e-3) / 1e9 / hbm, 4),
+                               "peak_source": src, "algorithmic_bytes_per_launch": int(by),
+                               "avg_launch_ms": round(avg, 4),
+                               "kernel_share": {k: round(v[1] / sum(x[1] for x in prof.values()),
+                                                         4) for k, v in prof.items()}}
+            res["algorithmic_bytes_per_cell_update"] = round(
+                rl.step_bytes3d(nC, info["n_faces"], info["n_cell_faces"], info["n_tiles"],
+                                info["n_borrowed"], prec, 2, 1) / (2 * nC), 1)
+        out[label] = res
+        s.close()
+    mesh.close()
+    if args.no_cpu or grp.ws > 1:
+        return out
+    # CPU restatement (single thread) on a bounded sample of the same family
+    from oracle import build as ob
+    from oracle import pyoracle as po
+    ob.build_oracle()
+    ns = min(n, 48)
+    ms_ = mg.tet_grid(ns, jitter=0.15, seed=20261205)
+    om = po.Mesh3(ms_["node_xyz"], ms_["faces"], ms_["face_cells"], ms_["zones"],
+                  ms_["n_cells"], ms_["c1_shift"])
+    qs = mg.taylor_green(ms_["cell_centroid"], mach=0.1)
+    p = po.params3(order=2, limiter=3, viscous=1, mu=mu, lam=-2.0 / 3.0 * mu,
+                   kappa=mu * 1.4 * cv / 0.71, cv=cv)
+    t1 = time.perf_counter()
+    po.rk2_3(om, p, qs, 1, 0.5)
+    secs = time.perf_counter() - t1
+    out["cpu_baseline"] = {"value": round(2 * ms_["n_cells"] / secs / 1e6, 3), "unit": UNIT,
+                           "cores": 1, "kind": "port",
+                           "sample": f"1 RK2 step of the {ns}^3 x 6 = {ms_['n_cells']}-cell "
+                                     f"mesh of the same family ({secs:.1f} s, FP64)"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -505,6 +596,9 @@ def main():
     ap.add_argument("--warm-train", type=int, default=32,
                     help="training cases of the learned warm start (0: no warm start)")
     ap.add_argument("--warm-steps", type=int, default=400)
+    ap.add_argument("--tgv-n", type=int, default=128,
+                    help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
+    ap.add_argument("--tgv-steps", type=int, default=10)
     args = ap.parse_args()
     ws, rank, local = _dist()
     workload = (f"isentropic vortex, periodic jittered Delaunay {args.n}x{args.n} "
@@ -540,6 +634,7 @@ def main():
     grp = _Group(ws)
     results, roof, nC = run_gpu(args, ws, rank, local, grp)
     batch_line = run_batch(args, ws, rank, grp) if args.batch_cases > 0 else None
+    tgv_line = run_tgv3d(args, grp) if args.tgv_n > 0 else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         m = _workload(args.n)
@@ -561,7 +656,7 @@ def main():
                     for k, v in results["e2e"].items()},
             "gpu_launches": fp32["launches"],
             "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks"),
-            "batch": batch_line}
+            "batch": batch_line, "tgv3d": tgv_line}
     print(json.dumps(line))
 
 

@@ -211,6 +211,8 @@ void mst_params3d_default(mst_params3d *p);
 typedef struct mst_ctx3d mst_ctx3d;
 typedef struct mst_ctx3d_info {
   int n_cells, n_faces, n_tiles, max_tile_faces;
+  int n_cell_faces;   /* CSR length */
+  int n_borrowed;     /* faces listed by a second tile (cut by tile borders) */
   size_t device_bytes;
 } mst_ctx3d_info;
 mst_status mst_ctx3d_create(const mst_mesh3d *m, const mst_params3d *p, mst_ctx3d **out);

@@ -34,6 +34,7 @@ struct mst_ctx3d {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   mst::DevMesh3 dm{};
   std::vector<int> cell_perm;  // file -> device
+  int n_cell_faces = 0, n_borrowed = 0;
   std::vector<void*> allocs;
   size_t bytes = 0;
   // FP64 state buffers (cur, stage, next) or float pairs for the FP32 path
@@ -372,6 +373,8 @@ mst_status mst_ctx3d_create(const mst_mesh3d* mesh, const mst_params3d* p, mst_c
     return fail3(MST_ECUDA, "memset failed");
   }
   c->cell_perm = L.cell_perm;
+  c->n_cell_faces = tot;
+  c->n_borrowed = (int)L.t_bor.size();
   *out = c.release();
   return MST_OK;
 }
@@ -398,6 +401,8 @@ mst_status mst_ctx3d_info_get(mst_ctx3d* c, mst_ctx3d_info* info) {
   info->n_faces = c->dm.n_faces;
   info->n_tiles = c->dm.n_tiles;
   info->max_tile_faces = c->dm.max_tile_faces;
+  info->n_cell_faces = c->n_cell_faces;
+  info->n_borrowed = c->n_borrowed;
   info->device_bytes = c->bytes;
   return MST_OK;
 }

@@ -66,7 +66,8 @@ class Params3D(C.Structure):
 
 class Ctx3DInfo(C.Structure):
     _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("n_tiles", C.c_int),
-                ("max_tile_faces", C.c_int), ("device_bytes", C.c_size_t)]
+                ("max_tile_faces", C.c_int), ("n_cell_faces", C.c_int), ("n_borrowed", C.c_int),
+                ("device_bytes", C.c_size_t)]
 
 
 class CaseParams(C.Structure):

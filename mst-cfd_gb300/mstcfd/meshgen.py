@@ -463,13 +463,21 @@ def tet_grid(n, length=2 * np.pi, jitter=0.15, seed=20261205):
     """Periodic [0, L)^3: an n^3 lattice of hexahedra, each split into 6
     tetrahedra along its main diagonal (the Kuhn subdivision, conforming
     across hexahedra), nodes moved by U(-jitter h, +jitter h) per axis.
-    6 n^3 cells, 12 n^3 triangular faces, all interior.  Vectorised (no
-    Python loop over cells) for the 128^3 x 6 = 12.6M-cell workload.
+    6 n^3 cells, 12 n^3 triangular faces, all interior.
+
+    The faces are enumerated analytically, vectorised over hexahedra: with
+    tet T_s = {0, e_s1, e_s1 + e_s2, 7} for an axis permutation s, its face
+    opposite e_s1 is shared with T_(s2, s1, s3) and its face opposite
+    e_s1 + e_s2 with T_(s1, s3, s2) (both in the same hexahedron); its face
+    opposite 7, on the hexahedron's lower side x_s3 = 0, is shared with
+    T_(s3, s1, s2) of the hexahedron below along s3.  Every hexahedron owns
+    its 6 interior faces and the 6 faces on its lower sides.
 
     Nodes are the (n+1)^3 unwrapped lattice points (the images at index n
     carry the jitter of index 0 plus L); every face lists its nodes in the
-    frame of its c0 and carries c1_shift = x(c0 frame) - x(c1 frame), a
-    multiple of L per axis.  Every area vector points into c0."""
+    frame of its c0 (the owning hexahedron's tet) and carries c1_shift =
+    x(c0 frame) - x(c1 frame), -L along s3 where the lower side wraps.
+    Every area vector points into c0."""
     n = int(n)
     if n < 2 or n > 128:
         raise ValueError("tet_grid: 2 <= n <= 128")
@@ -477,68 +485,67 @@ def tet_grid(n, length=2 * np.pi, jitter=0.15, seed=20261205):
     n1 = n + 1
     rng = np.random.default_rng(seed)
     jit = rng.uniform(-jitter, jitter, (n ** 3, 3))
-    g = np.stack(np.meshgrid(np.arange(n1), np.arange(n1), np.arange(n1), indexing="ij"),
-                 -1).reshape(-1, 3)
-    wrap = ((g[:, 0] % n) * n + (g[:, 1] % n)) * n + (g[:, 2] % n)
-    xyz = (g + jit[wrap]) * h
-    # rows: (cube, tet, face) -> the face's 3 cube corners
-    corner = np.array([[c & 1, (c >> 1) & 1, (c >> 2) & 1] for c in range(8)], np.int64)
-    tri = []
+    ax = np.arange(n1)
+    gi, gj, gk = np.meshgrid(ax, ax, ax, indexing="ij")
+    wrap = ((gi % n) * n + (gj % n)) * n + (gk % n)
+    xyz = (np.stack([gi, gj, gk], -1).reshape(-1, 3) + jit[wrap.ravel()]) * h
+    del gi, gj, gk, wrap
+    # tet index of each axis permutation (the order of _KUHN)
+    sig = []
     for t in _KUHN:
-        tri += [[t[0], t[1], t[2]], [t[0], t[1], t[3]], [t[0], t[2], t[3]], [t[1], t[2], t[3]]]
-    tri = np.array(tri, np.int64)                       # [24][3] corners
+        a1 = int(np.log2(t[1]))
+        a2 = int(np.log2(t[2] - t[1]))
+        sig.append((a1, a2, 3 - a1 - a2))
+    idx = {s_: i for i, s_ in enumerate(sig)}
+    e = [1, 2, 4]  # corner bit of each axis
+    local = []  # (tet, partner tet, corners (3), lower side axis or -1)
+    for i, (s1, s2, s3) in enumerate(sig):
+        for corners, partner in (((0, e[s1] + e[s2], 7), (s2, s1, s3)),
+                                 ((0, e[s1], 7), (s1, s3, s2))):
+            j = idx[partner]
+            if i < j:
+                local.append((i, j, corners, -1))
+        local.append((i, idx[(s3, s1, s2)], (0, e[s1], e[s1] + e[s2]), s3))
+    assert len(local) == 12
     cube = np.arange(n ** 3, dtype=np.int64)
-    base = np.stack([cube // (n * n), (cube // n) % n, cube % n], 1)  # [n^3][3]
-    # lattice coordinates of every row's 3 nodes: [n^3, 24, 3(node), 3(axis)]
-    lat = base[:, None, None, :] + corner[tri][None, :, :, :]
-    lat = lat.reshape(-1, 3, 3)
-    uid = (lat[..., 0] * n1 + lat[..., 1]) * n1 + lat[..., 2]          # unwrapped ids
-    wid = ((lat[..., 0] % n) * n + lat[..., 1] % n) * n + lat[..., 2] % n
-    del lat
-    cell = np.repeat(np.arange(6 * n ** 3, dtype=np.int64), 4)
-    ws = np.sort(wid, 1)
-    key = (ws[:, 0] << 42) | (ws[:, 1] << 21) | ws[:, 2]
-    del ws
-    order = np.argsort(key, kind="stable")
-    a, b = order[0::2], order[1::2]
-    if not np.array_equal(key[a], key[b]):
-        raise RuntimeError("tet_grid: unpaired face")
-    del key, order
-    # faces in c0 order (the row of the lower cell comes first)
-    f0 = np.minimum(a, b)
-    f1 = np.maximum(a, b)
-    o = np.argsort(f0, kind="stable")
-    f0, f1 = f0[o], f1[o]
-    c0, c1 = cell[f0], cell[f1]
-    nodes = uid[f0]                                       # c0's frame
-    # c1_shift: the same wrapped node in both rows
-    w0 = wid[f0, 0]
-    hit = (wid[f1] == w0[:, None])
-    j1 = np.argmax(hit, 1)
-    u1 = uid[f1, j1]
-    l0 = np.stack([nodes[:, 0] // (n1 * n1), (nodes[:, 0] // n1) % n1, nodes[:, 0] % n1], 1)
-    l1 = np.stack([u1 // (n1 * n1), (u1 // n1) % n1, u1 % n1], 1)
-    shift = ((l0 - l1) // n).astype(np.float64) * length
-    # orientation: the area vector (n1-n0) x (n2-n0) points into c0
-    p0, p1, p2 = xyz[nodes[:, 0]], xyz[nodes[:, 1]], xyz[nodes[:, 2]]
-    nrm = np.cross(p1 - p0, p2 - p0)
-    fc = (p0 + p1 + p2) / 3.0
-    cubes0 = c0 // 6
-    t0 = c0 % 6
-    kuhn = np.array(_KUHN, np.int64)
-    cc = (base[cubes0][:, None, :] + corner[kuhn[t0]]).astype(np.float64)  # lattice corners
-    cen = ((cc + jit[(((cc[..., 0] % n) * n + cc[..., 1] % n) * n + cc[..., 2] % n)
-                     .astype(np.int64)]) * h).mean(1)
-    flip = np.einsum("ij,ij->i", nrm, fc - cen) > 0
-    nodes[flip, 1], nodes[flip, 2] = nodes[flip, 2].copy(), nodes[flip, 1].copy()
-    nF = len(nodes)
+    ci, cj, ck = cube // (n * n), (cube // n) % n, cube % n
+    base_u = (ci * n1 + cj) * n1 + ck
+    coff = lambda c: (c & 1) * n1 * n1 + ((c >> 1) & 1) * n1 + ((c >> 2) & 1)
+    nF = 12 * n ** 3
+    faces = np.empty((n ** 3, 12, 3), np.int64)
+    fc = np.empty((n ** 3, 12, 2), np.int64)
+    shift = np.zeros((n ** 3, 12, 3))
+    cidx = (ci, cj, ck)
+    for f, (t0, t1, corners, side) in enumerate(local):
+        for j, c in enumerate(corners):
+            faces[:, f, j] = base_u + coff(c)
+        fc[:, f, 0] = 6 * cube + t0
+        if side < 0:
+            fc[:, f, 1] = 6 * cube + t1
+        else:
+            nb = list(cidx)
+            nb[side] = (cidx[side] - 1) % n
+            fc[:, f, 1] = 6 * ((nb[0] * n + nb[1]) * n + nb[2]) + t1
+            shift[:, f, side] = np.where(cidx[side] == 0, -length, 0.0)
+    faces = faces.reshape(nF, 3)
+    fc = fc.reshape(nF, 2)
+    shift = shift.reshape(nF, 3)
     # cell centroids (mean of the 4 nodes, own frame)
-    allc = np.arange(6 * n ** 3, dtype=np.int64)
-    ccl = (base[allc // 6][:, None, :] + corner[kuhn[allc % 6]]).astype(np.int64)
-    cwr = ((ccl[..., 0] % n) * n + ccl[..., 1] % n) * n + ccl[..., 2] % n
-    centroid = ((ccl + jit[cwr]) * h).mean(1)
-    return {"node_xyz": xyz, "faces": nodes.astype(np.int32),
-            "face_cells": np.stack([c0, c1], 1).astype(np.int32),
+    kuhn = np.array(_KUHN, np.int64)
+    offs = np.array([coff(c) for c in range(8)], np.int64)
+    cn = base_u[:, None, None] + offs[kuhn][None, :, :]         # [n^3, 6, 4]
+    centroid = xyz[cn.reshape(-1, 4)].mean(1)
+    del cn
+    # orientation: the area vector (n1-n0) x (n2-n0) points into c0
+    p0, p1, p2 = xyz[faces[:, 0]], xyz[faces[:, 1]], xyz[faces[:, 2]]
+    nrm = np.cross(p1 - p0, p2 - p0)
+    ctr = (p0 + p1 + p2) / 3.0
+    del p0, p1, p2
+    flip = np.einsum("ij,ij->i", nrm, ctr - centroid[fc[:, 0]]) > 0
+    del nrm, ctr
+    faces[flip, 1], faces[flip, 2] = faces[flip, 2].copy(), faces[flip, 1].copy()
+    return {"node_xyz": xyz, "faces": faces.astype(np.int32),
+            "face_cells": fc.astype(np.int32),
             "zones": np.array([[3, 1, nF, INTERIOR]], np.int32), "n_cells": 6 * n ** 3,
             "c1_shift": shift, "cell_centroid": centroid}
 

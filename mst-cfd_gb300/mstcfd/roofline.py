@@ -52,3 +52,44 @@ def step_bytes(info, precision, order, rk2=True, cfl=True):
     if cfl:
         b += kernel_bytes(info, precision, order, "k_spectral_dt")
     return b
+
+
+def kernel_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precision, order,
+                   viscous, kernel, stage=0):
+    """Algorithmic bytes of one launch of a 3D kernel (kernels3d.inc) under
+    R1-R4.  FP32 path (precision 2): geometry and gradient in FP32, the
+    state as float pairs (20 B hi + 20 B lo per cell); FP64 paths: FP64
+    geometry, gradient and state (40 B per cell)."""
+    nC, nF, tot = n_cells, n_faces, n_cell_faces
+    s = 4 if precision == 2 else 8
+    if kernel.startswith("k3_flux_update"):
+        # per face: c0/c1, info, area vector, and for order 2 the two
+        # reconstruction offsets (+ eta0 when viscous)
+        faces = nF * (8 + 4 + 3 * s + ((6 * s + (s if viscous else 0)) if order == 2 else 0))
+        tiles = 8 * (n_tiles + 1) + 4 * n_borrowed
+        if precision == 2:
+            # state hi (reconstruction), lo (update), Q^n pair on stage 1,
+            # new pair written; 1/V pair; CSR; gradient
+            cells = nC * (20 + 20 + 40 + 8 + 4) + (nC * 40 if stage == 1 else 0)
+        else:
+            cells = nC * (40 + 40 + 8 + 4) + (nC * 40 if stage == 1 else 0)
+        if order == 2:
+            cells += nC * 15 * s
+        return faces + tiles + cells + 4 * tot
+    if kernel.startswith("k3_gradient"):
+        qs = 20 if precision == 2 else 40
+        return nC * (qs + 4 + 8 + 15 * s) + tot * (4 + 2 * s + 3 * s) + 8 * ((nC + 255) // 256)
+    return 0
+
+
+def step_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precision, order,
+                 viscous):
+    """Algorithmic bytes of one RK2 step of the 3D path (two stages)."""
+    b = 0
+    for st in (0, 1):
+        b += kernel_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precision,
+                            order, viscous, "k3_flux_update", stage=st)
+        if order == 2:
+            b += kernel_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precision,
+                                order, viscous, "k3_gradient")
+    return b
