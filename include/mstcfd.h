@@ -375,11 +375,18 @@ typedef struct mst_implicit_params {
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
   int autotune;     /* time the sweep block sizes once and keep the fastest */
-  int reserved[5];
+  /* FP32 sweeps (production paths): the off-diagonal flux differences and
+   * spectral radii in FP32 on FP32 copies of the state and of dQ; the
+   * diagonal, its inversion and the state update stay FP64.  The residual
+   * that decides convergence is unchanged, so the converged state meets
+   * the same tolerance. */
+  int sweep_fp32;
+  int reserved[4];
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,
- * fp32_until 0, max_iter 20000, graph_iters 20, autotune on. */
+ * fp32_until 0, max_iter 20000, graph_iters 20, autotune on,
+ * sweep_fp32 off. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {

@@ -78,6 +78,8 @@ struct mst_batch {
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
+  float4* dqf = nullptr;         // FP32 sweeps: dQ* / dQ in FP32
+  bool sweep32 = false;
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
   // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
   // lo is set, FP64 afterwards; the sweeps are FP64 throughout
@@ -111,7 +113,7 @@ mst_status bupload(mst_batch* b, T** p, const std::vector<T>& v) {
 double4_32a* qbuf(mst_batch* b, int which) { return which ? b->ctx->q_new : b->ctx->q_old; }
 // FP32 copy of the state, kept where an FP32 residual reads it
 float4* qfbuf(mst_batch* b, int which) {
-  if (b->ctx->p.precision != MST_PREC_FP32 && !b->lo) return nullptr;
+  if (b->ctx->p.precision != MST_PREC_FP32 && !b->lo && !b->sweep32) return nullptr;
   return which ? b->ctx->qf_new : b->ctx->qf_old;
 }
 
@@ -175,6 +177,12 @@ mst::LusgsArgs sweep_args(mst_batch* b, int which) {
   la.omega = b->ip.omega;
   la.conv_iter = b->conv_iter;
   la.iter = b->iter;
+  if (b->sweep32) {
+    la.qf = qfbuf(b, which);
+    la.dqf = b->dqf;
+    la.case_tab_f = b->case_tab_f;
+    la.mu_f = (float)c->p.mu;
+  }
   return la;
 }
 
@@ -345,6 +353,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
                              "(0 on the exact path)");
   std::unique_ptr<mst_batch> b(new mst_batch());
   b->ip = *ip;
+  b->sweep32 = ip->sweep_fp32 != 0 && p->precision != MST_PREC_FP64_EXACT;
   b->n_cases = n_cases;
   std::vector<const mst::HostMesh*> parts;
   for (int k = 0; k < n_cases; ++k) {
@@ -432,6 +441,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
                        (p->precision == MST_PREC_FP32 ? sizeof(float) : sizeof(double)))) ||
       (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
+      (st = balloc(b.get(), &b->dqf, b->sweep32 ? sizeof(float4) * (size_t)nC : 0)) ||
       (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
                                             ? sizeof(float) * 8 * (size_t)nC : 0)) ||
       (st = reset_progress(b.get()))) {
@@ -487,7 +497,7 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   b->lo = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
   b->lo_below = 0;
   b->lo_since = 0;
-  if (b->lo) {
+  if (b->lo || b->sweep32) {
     cudaError_t e = mst::fast::launch_to_f32(b->ctx->q_old, b->ctx->qf_old, b->ctx->dm.n_cells,
                                              b->ctx->stream);
     if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, cudaGetErrorString(e));

@@ -146,6 +146,12 @@ struct LusgsArgs {
   double omega;
   const int* conv_iter;    // [n_cases] converged cases keep their state
   const int* iter;         // iteration counter (already advanced by the norms)
+  // FP32 sweeps (dqf != nullptr): FP32 state copy, dQ* / dQ in FP32, the
+  // per-case coefficients in FP32
+  const float4* qf;
+  float4* dqf;
+  const float* case_tab_f;
+  float mu_f;
 };
 
 // Per-case residual norms and the CFL of the next iteration, one block per

@@ -4,14 +4,19 @@
 
 namespace mst {
 
-// 3D mesh in device order (mesh3d.hpp DevLayout3D); vectors of 3 packed
-// (x, y, z) per face or cell-face, in FP64 and FP32 copies
+// Gradient record per cell: [3][5] plus one pad, so that a cell's gradient
+// is 64 B (FP32) or 128 B (FP64), loaded and stored as aligned vectors.
+constexpr int kGrad3 = 16;
+
+// 3D mesh in device order (mesh3d.hpp DevLayout3D): FP64 vectors of 3
+// packed (x, y, z) per face or cell-face, and FP32 copies packed in float4
 struct DevMesh3 {
   int n_cells, n_faces, n_tiles, max_tile_faces;
   const int2* f_c0c1;
   const int* f_info;
   const double *f_dir, *f_r0, *f_r1, *f_eta;
-  const float *f_dir32, *f_r0_32, *f_r1_32, *f_eta32;
+  // FP32 copies packed for one 16-byte load each: (S, eta0), (r0, 0), (r1, 0)
+  const float4 *f_dir_eta32, *f_r0_32, *f_r1_32;
   const double* c_vol;
   const double* c_ivol;     // 1/V
   const float2* c_ivol_ff;  // 1/V as a float pair
@@ -19,9 +24,10 @@ struct DevMesh3 {
   const int* cf_slot;       // tile slot << 1 | (cell is c1 of the face)
   const int* cf_nb;         // neighbour device cell, -1 on boundary faces
   const double* cf_w;       // [tot][2] face-value weights (self, neighbour)
-  const float* cf_w32;
   const double* cf_dir;     // [tot][3] outward area vector
-  const float* cf_dir32;
+  // FP32 copies: (outward S, self weight) and the neighbour weight
+  const float4* cf_dw32;
+  const float* cf_w1_32;
   const int *t_own_ptr, *t_bor_ptr, *t_bor;
 };
 
@@ -44,7 +50,7 @@ struct Step3Args {
   const float* ph1;
   const float4* pl4;
   const float* pl1;
-  const void* grad;       // [nC][3][5] in the path's precision
+  const void* grad;       // [nC][kGrad3] in the path's precision ([3][5] + pad)
   double* r_out;          // [nC][5] residual (residual-only launches)
   const double* scal;     // device [0] = dt (FP64 paths)
   const float* dt_ff;     // device dt as a float pair (FP32 path)

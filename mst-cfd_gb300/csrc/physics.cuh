@@ -298,4 +298,55 @@ __host__ __device__ __forceinline__ void roe_flux(const T ql[4], const T qr[4],
   }
 }
 
+// The same Roe flux for the production paths: |A| dQ in closed form as the
+// sum over the waves of |lambda_k| alpha_k r_k, with the wave strengths
+// from the primitive jumps and the Roe-averaged state (equal to
+// R |Lambda| R^-1 dQ of roe_flux for that state, without the 4x4 inverse
+// and the two 4x4 products); the same entropy-fixed eigenvalues, physical
+// fluxes and EOR denominators.  Not used by the exact path.
+template <class T>
+__host__ __device__ __forceinline__ void roe_flux_fast(const T ql[4], const T qr[4], int d,
+                                                       T f[4]) {
+  const T eor = T(1e-10);
+  const int t = 1 - d;
+  const T irL = T(1) / ql[0], irR = T(1) / qr[0];
+  const T D = sqrt(fabs(qr[0] * irL));
+  const T iD = T(1) / (T(1) + D);
+  const T uL[2] = {ql[1] * irL, ql[2] * irL}, uR[2] = {qr[1] * irR, qr[2] * irR};
+  const T u[2] = {(uL[0] + D * uR[0]) * iD, (uL[1] + D * uR[1]) * iD};
+  const T pL = th_p(ql), pR = th_p(qr);
+  const T hL = (ql[3] + pL) * irL, hR = (qr[3] + pR) * irR;
+  const T H = (hL + D * hR) * iD;
+  const T ke = T(0.5) * (u[0] * u[0] + u[1] * u[1]);
+  const T a2 = fabs(Gas<T>::gm1() * (H - ke));
+  const T a = sqrt(a2);
+  const T ud = u[d], ut = u[t];
+  const T l1 = entropy_fix(fabs(ud - a)), l2 = entropy_fix(fabs(ud)),
+          l4 = entropy_fix(fabs(ud + a));
+  const T rt = D * ql[0];
+  const T dp = pR - pL, dud = uR[d] - uL[d], dut = uR[t] - uL[t];
+  const T ia2 = T(1) / a2;
+  const T w1 = l1 * (T(0.5) * (dp - rt * a * dud) * ia2);
+  const T w4 = l4 * (T(0.5) * (dp + rt * a * dud) * ia2);
+  const T w2 = l2 * ((qr[0] - ql[0]) - dp * ia2);
+  const T w3 = l2 * (rt * dut);
+  T dis[4];
+  dis[0] = w1 + w2 + w4;
+  dis[1 + d] = w1 * (ud - a) + w2 * ud + w4 * (ud + a);
+  dis[1 + t] = (w1 + w2 + w4) * ut + w3;
+  dis[3] = w1 * (H - ud * a) + w2 * ke + w4 * (H + ud * a) + w3 * ut;
+  const T iL = T(1) / (ql[0] + eor), iR = T(1) / (qr[0] + eor);
+  T FL[4], FR[4];
+  FL[0] = ql[1 + d];
+  FR[0] = qr[1 + d];
+  FL[1 + d] = ql[1 + d] * ql[1 + d] * iL + pL;
+  FR[1 + d] = qr[1 + d] * qr[1 + d] * iR + pR;
+  FL[1 + t] = ql[1] * ql[2] * iL;
+  FR[1 + t] = qr[1] * qr[2] * iR;
+  FL[3] = hL * ql[1 + d];
+  FR[3] = hR * qr[1 + d];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) f[k] = T(0.5) * (FL[k] + FR[k]) - T(0.5) * dis[k];
+}
+
 }  // namespace mst

@@ -328,21 +328,35 @@ mst_status mst_ctx3d_create(const mst_mesh3d* mesh, const mst_params3d* p, mst_c
     const float hi = (float)ivol[i];
     ivff[i] = make_float2(hi, (float)(ivol[i] - (double)hi));
   }
+  // packed FP32 copies of the geometry
+  std::vector<float4> fde(nF), fr0(nF), fr1(nF), cdw(tot);
+  std::vector<float> cw1(tot);
+  for (int f = 0; f < nF; ++f) {
+    const double* dv = &L.f_dir[3 * (size_t)f];
+    const double* a0 = &L.f_r0[3 * (size_t)f];
+    const double* a1 = &L.f_r1[3 * (size_t)f];
+    fde[f] = make_float4((float)dv[0], (float)dv[1], (float)dv[2], (float)L.f_eta[f]);
+    fr0[f] = make_float4((float)a0[0], (float)a0[1], (float)a0[2], 0.0f);
+    fr1[f] = make_float4((float)a1[0], (float)a1[1], (float)a1[2], 0.0f);
+  }
+  for (int k = 0; k < tot; ++k) {
+    const double* dv = &L.cf_dir[3 * (size_t)k];
+    cdw[k] = make_float4((float)dv[0], (float)dv[1], (float)dv[2], (float)L.cf_w[2 * (size_t)k]);
+    cw1[k] = (float)L.cf_w[2 * (size_t)k + 1];
+  }
   mst_status st = MST_OK;
   if ((st = upload3(c.get(), &d.f_c0c1, c0c1)) || (st = upload3(c.get(), &d.f_info, L.f_info)) ||
       (st = upload3(c.get(), &d.f_dir, L.f_dir)) || (st = upload3(c.get(), &d.f_r0, L.f_r0)) ||
       (st = upload3(c.get(), &d.f_r1, L.f_r1)) || (st = upload3(c.get(), &d.f_eta, L.f_eta)) ||
-      (st = upload3(c.get(), &d.f_dir32, L.f_dir)) ||
-      (st = upload3(c.get(), &d.f_r0_32, L.f_r0)) ||
-      (st = upload3(c.get(), &d.f_r1_32, L.f_r1)) ||
-      (st = upload3(c.get(), &d.f_eta32, L.f_eta)) || (st = upload3(c.get(), &d.c_vol, L.c_vol)) ||
+      (st = upload3(c.get(), &d.f_dir_eta32, fde)) ||
+      (st = upload3(c.get(), &d.f_r0_32, fr0)) || (st = upload3(c.get(), &d.f_r1_32, fr1)) ||
+      (st = upload3(c.get(), &d.c_vol, L.c_vol)) ||
       (st = upload3(c.get(), &d.c_ivol, ivol)) || (st = upload3(c.get(), &d.c_ivol_ff, ivff)) ||
       (st = upload3(c.get(), &d.c_ptr, L.c_ptr)) ||
       (st = upload3(c.get(), &d.cf_slot, L.cf_slot)) ||
       (st = upload3(c.get(), &d.cf_nb, L.cf_nb)) || (st = upload3(c.get(), &d.cf_w, L.cf_w)) ||
-      (st = upload3(c.get(), &d.cf_w32, L.cf_w)) ||
       (st = upload3(c.get(), &d.cf_dir, L.cf_dir)) ||
-      (st = upload3(c.get(), &d.cf_dir32, L.cf_dir)) ||
+      (st = upload3(c.get(), &d.cf_dw32, cdw)) || (st = upload3(c.get(), &d.cf_w1_32, cw1)) ||
       (st = upload3(c.get(), &d.t_own_ptr, L.t_own_ptr)) ||
       (st = upload3(c.get(), &d.t_bor_ptr, L.t_bor_ptr)) ||
       (st = upload3(c.get(), &d.t_bor, L.t_bor))) {
@@ -361,7 +375,7 @@ mst_status mst_ctx3d_create(const mst_mesh3d* mesh, const mst_params3d* p, mst_c
   }
   if (st || (st = alloc3(c.get(), &c->qtmp, 5 * (size_t)nC)) ||
       (st = alloc3(c.get(), (char**)&c->grad,
-                   15 * (size_t)nC * (pairs ? sizeof(float) : sizeof(double)))) ||
+                   mst::kGrad3 * (size_t)nC * (pairs ? sizeof(float) : sizeof(double)))) ||
       (st = alloc3(c.get(), &c->dt_part, nb)) || (st = alloc3(c.get(), &c->scal, 2)) ||
       (st = alloc3(c.get(), &c->dt_ff, 2)) || (st = alloc3(c.get(), &c->ke_part, 2 * (size_t)nb)) ||
       (st = alloc3(c.get(), &c->ke_out, 2))) {
@@ -449,7 +463,8 @@ mst_status mst_ctx3d_gradient(mst_ctx3d* c, double* g) {
   mst::Step3Args a = args3(c, c->cur, -1, -1, 0);
   C3(grad3(c, a, nullptr));
   const int nC = c->dm.n_cells;
-  std::vector<double> gd(15 * (size_t)nC);
+  const int W = mst::kGrad3;
+  std::vector<double> gd(W * (size_t)nC);
   C3(cudaStreamSynchronize(c->stream));
   if (f32(c)) {
     std::vector<float> gf(gd.size());
@@ -459,7 +474,7 @@ mst_status mst_ctx3d_gradient(mst_ctx3d* c, double* g) {
     C3(cudaMemcpy(gd.data(), c->grad, gd.size() * sizeof(double), cudaMemcpyDeviceToHost));
   }
   for (int f = 0; f < nC; ++f)
-    std::memcpy(g + 15 * (size_t)f, gd.data() + 15 * (size_t)c->cell_perm[f], 15 * sizeof(double));
+    std::memcpy(g + 15 * (size_t)f, gd.data() + W * (size_t)c->cell_perm[f], 15 * sizeof(double));
   return MST_OK;
 }
 

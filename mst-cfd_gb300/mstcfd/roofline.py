@@ -64,8 +64,12 @@ def kernel_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precisio
     s = 4 if precision == 2 else 8
     if kernel.startswith("k3_flux_update"):
         # per face: c0/c1, info, area vector, and for order 2 the two
-        # reconstruction offsets (+ eta0 when viscous)
-        faces = nF * (8 + 4 + 3 * s + ((6 * s + (s if viscous else 0)) if order == 2 else 0))
+        # reconstruction offsets (+ eta0 when viscous); the FP32 copies are
+        # packed as float4 (S, eta0), (r0, 0), (r1, 0)
+        if precision == 2:
+            faces = nF * (8 + 4 + 16 + (32 if order == 2 else 0))
+        else:
+            faces = nF * (8 + 4 + 3 * s + ((6 * s + (s if viscous else 0)) if order == 2 else 0))
         tiles = 8 * (n_tiles + 1) + 4 * n_borrowed
         if precision == 2:
             # state hi (reconstruction), lo (update), Q^n pair on stage 1,
@@ -74,11 +78,13 @@ def kernel_bytes3d(n_cells, n_faces, n_cell_faces, n_tiles, n_borrowed, precisio
         else:
             cells = nC * (40 + 40 + 8 + 4) + (nC * 40 if stage == 1 else 0)
         if order == 2:
-            cells += nC * 15 * s
+            cells += nC * 16 * s  # gradient record: [3][5] + pad
         return faces + tiles + cells + 4 * tot
     if kernel.startswith("k3_gradient"):
         qs = 20 if precision == 2 else 40
-        return nC * (qs + 4 + 8 + 15 * s) + tot * (4 + 2 * s + 3 * s) + 8 * ((nC + 255) // 256)
+        # per cell-face: neighbour, outward S and the two weights (FP32:
+        # float4 (S, w0) + w1)
+        return nC * (qs + 4 + 8 + 16 * s) + tot * (4 + 5 * s) + 8 * ((nC + 255) // 256)
     return 0
 
 

@@ -9,7 +9,8 @@ residual with every order / limiter / the viscous term, on a periodic
 mesh and on a box with inlet, outlet, wall and symmetry zones; RK2 steps
 with the global CFL step); FP64 with FMA within 1e-12 and the FP32 path
 within FP32 rounding of it; FP32 conserves mass to float-pair accuracy;
-the viscous term decays a shear wave at the analytic rate; the Taylor-Green
+the viscous term decays a shear wave at the rate its gradient operator
+predicts; the Taylor-Green
 kinetic energy decays, FP32 tracking FP64.
 """
 import numpy as np
@@ -199,9 +200,14 @@ def test_gpu3d_fp32_conserves_mass():
 @pytest.mark.gpu
 def test_gpu3d_shear_wave_viscous_decay():
     """u = U sin(y) (y in radians), periodic: kinetic energy decays as
-    exp(-2 nu t) (k = 1); the inviscid run keeps it to within its numerical
-    dissipation, so the viscous decay is taken relative to it."""
+    exp(-2 nu g t), g = 1 for the exact gradient.  The reference's gradient
+    (Green-Gauss with eta0-weighted face values, RhoSolver.cpp:430-453) is
+    not exact on the Kuhn tetrahedra: it overestimates |grad u|^2 by ~21%
+    (spurious cross-derivatives, no convergence with refinement), so g is
+    taken from that operator applied to the initial field (the checker's
+    gradient).  The inviscid run's own numerical dissipation is divided out."""
     from mstcfd import meshgen as mg
+    from oracle import pyoracle as po
     m = _tgv_mesh(16, jitter=0.1)
     xyz = m["cell_centroid"]
     U, nu = 0.05, 0.02
@@ -209,6 +215,11 @@ def test_gpu3d_shear_wave_viscous_decay():
     u = U * np.sin(xyz[:, 1])
     p = np.full(len(xyz), 1 / GAMMA)
     q0 = np.stack([rho, rho * u, 0 * u, 0 * u, p / 0.4 + 0.5 * rho * u * u], 1)
+    om = _oracle(m)
+    vol = om.arrays()["cell_vol"]
+    gu = po.gradient3(om, q0)[:, :, 1]
+    g = (vol * (gu ** 2).sum(1)).sum() / (vol * (U * np.cos(xyz[:, 1])) ** 2).sum()
+    assert 1.0 < g < 1.4
     ke = {}
     for visc in (0, 1):
         s = _solver(m, precision=1, order=2, limiter=0, viscous=visc, mu=nu, lambda_=-2 * nu / 3,
@@ -221,8 +232,8 @@ def test_gpu3d_shear_wave_viscous_decay():
         s.close()
     assert ke[0][2] == 2.0 and ke[1][2] == 2.0
     ratio = (ke[1][1] / ke[1][0]) / (ke[0][1] / ke[0][0])
-    # within 5% of the analytic decay (Green-Gauss gradients on h = 0.39)
-    assert abs(ratio - np.exp(-2 * nu * 2.0)) < 0.05 * (1 - np.exp(-2 * nu * 2.0))
+    want = np.exp(-2 * nu * g * 2.0)
+    assert abs(ratio - want) < 0.05 * (1 - want)
 
 
 @pytest.mark.gpu
