@@ -304,6 +304,12 @@ def _wedge_cases(n_cases, lo, hi):
              p["reynolds"]) for p in mg.wedge_family(n_cases, cells=(lo, hi))]
 
 
+# temperature floor of the batched LU-SGS solves, p >= P_FLOOR rho (1.4% of
+# the free stream's p / rho): a near-vacuum cell at the slip / no-slip
+# corner of a ramp otherwise rejects every update and freezes its case
+P_FLOOR = 0.01
+
+
 def run_batch(args, ws, rank, grp):
     """Cold-start batched LU-SGS solve of the wedge family to L2 1e-8.  With
     N ranks the cases are split by greedy size balancing, each rank solves
@@ -323,7 +329,7 @@ def run_batch(args, ws, rank, grp):
         cases.append((mesh, batch.case_params(mg.freestream(mach), mu=mu, lambda_=-2 / 3 * mu,
                                               kappa=mu * gamma * cv / 0.72, cv=cv)))
         q0.append(mg.freestream(mach, mesh.n_cells))
-    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters),
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, p_floor=P_FLOOR),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q0)
     grp.barrier()
@@ -350,14 +356,15 @@ def run_batch(args, ws, rank, grp):
            "workload": (f"{len(cases)} compression ramps, {args.batch_cells[0]}-"
                         f"{args.batch_cells[1]} triangles each, Mach U[1.5,3], angle U[5,15] deg "
                         f"(attached shocks), "
-                        f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, cap "
+                        f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, temperature floor p >= "
+                        f"{P_FLOOR} rho, cap "
                         f"{args.batch_iters} iterations"),
            "warm": None}
     q_cold = b.state()
     conv_cold = conv
     b.close()
     # the same cold start with the FP32 residual until 1e-3 (then FP64)
-    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1),
+    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1, p_floor=P_FLOOR),
                      flux=1, order=2, limiter=1, precision=1, viscous=1)
     bm.set_state(q0)
     grp.barrier()
@@ -395,7 +402,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
                                 m["n_cells"])
         train.append((p, m, mesh, cp))
     tb = batch.Batch([(mesh, cp) for _, _, mesh, cp in train],
-                     implicit=dict(max_iter=args.batch_iters),
+                     implicit=dict(max_iter=args.batch_iters, p_floor=P_FLOOR),
                      flux=1, order=2, limiter=1, precision=1, viscous=1)
     tb.set_state([mg.freestream(p["mach"], mesh.n_cells) for p, _, mesh, _ in train])
     tb.solve()
@@ -427,7 +434,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
     q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
     infer_s = time.perf_counter() - t2
     gemm = _gemm_at_scale(net, feats)
-    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1),
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1, p_floor=P_FLOOR),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q_warm)
     t3 = time.perf_counter()

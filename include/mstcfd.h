@@ -381,12 +381,17 @@ typedef struct mst_implicit_params {
    * that decides convergence is unchanged, so the converged state meets
    * the same tolerance. */
   int sweep_fp32;
-  int reserved[4];
+  /* temperature floor (0: off): an updated state with p < p_floor * rho
+   * gets its internal energy raised to p = p_floor * rho (density and
+   * momentum kept).  Without it a near-vacuum cell at a slip / no-slip
+   * corner rejects every update (positivity) and freezes its case. */
+  double p_floor;
+  int reserved[2];
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,
  * fp32_until 0, max_iter 20000, graph_iters 20, autotune on,
- * sweep_fp32 off. */
+ * sweep_fp32 off, p_floor 0. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {

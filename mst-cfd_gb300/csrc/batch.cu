@@ -177,6 +177,7 @@ mst::LusgsArgs sweep_args(mst_batch* b, int which) {
   la.omega = b->ip.omega;
   la.conv_iter = b->conv_iter;
   la.iter = b->iter;
+  la.p_floor = b->ip.p_floor;
   if (b->sweep32) {
     la.qf = qfbuf(b, which);
     la.dqf = b->dqf;
@@ -349,7 +350,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1))
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
-                             "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0 "
+                             "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0, p_floor >= 0 "
                              "(0 on the exact path)");
   std::unique_ptr<mst_batch> b(new mst_batch());
   b->ip = *ip;

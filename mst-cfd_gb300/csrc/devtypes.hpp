@@ -152,6 +152,7 @@ struct LusgsArgs {
   float4* dqf;
   const float* case_tab_f;
   float mu_f;
+  double p_floor;          // temperature floor p >= p_floor * rho (0: off)
 };
 
 // Per-case residual norms and the CFL of the next iteration, one block per

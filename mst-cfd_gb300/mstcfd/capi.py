@@ -79,7 +79,8 @@ class ImplicitParams(C.Structure):
     _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double),
                 ("tol", C.c_double), ("freeze_tol", C.c_double), ("fp32_until", C.c_double),
                 ("max_iter", C.c_int), ("graph_iters", C.c_int),
-                ("autotune", C.c_int), ("sweep_fp32", C.c_int), ("reserved", C.c_int * 4)]
+                ("autotune", C.c_int), ("sweep_fp32", C.c_int), ("p_floor", C.c_double),
+                ("reserved", C.c_int * 2)]
 
 
 class BatchInfo(C.Structure):

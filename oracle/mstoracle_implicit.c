@@ -187,6 +187,12 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
             if (!ok) alpha *= 0.5;
           }
           for (j = 0; j < 4; ++j) qn[4 * (size_t)c + j] = ok ? n[j] : qc[j];
+          if (ip->p_floor > 0.0) {
+            double *w = qn + 4 * (size_t)c;
+            const double ke = 0.5 * (w[1] * w[1] + w[2] * w[2]) / w[0];
+            const double pw = kGm1 * (w[3] - ke);
+            if (pw < ip->p_floor * w[0]) w[3] = ke + ip->p_floor * w[0] / kGm1;
+          }
         }
       }
     memcpy(q, qn, sizeof(double) * 4 * (size_t)nC);

@@ -17,6 +17,9 @@ typedef struct om_lusgs_params {
   /* convergence: from the first iteration with L2 <= tol * L2_first on,
    * the state is kept (0: never) */
   double tol;
+  /* temperature floor: an updated state with p < p_floor * rho gets its
+   * internal energy raised to p = p_floor * rho (0: off) */
+  double p_floor;
 } om_lusgs_params;
 
 /* niter LU-SGS iterations of one case in place (corrected-mode residual of

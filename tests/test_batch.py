@@ -120,15 +120,19 @@ def test_oracle_limiter_freezing_removes_the_stall(freeze):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("freeze", [0.0, 0.9], ids=["live", "frozen"])
+@pytest.mark.parametrize("freeze,p_floor", [(0.0, 0.0), (0.9, 0.0), (0.0, 0.75)],
+                         ids=["live", "frozen", "floor"])
 @pytest.mark.parametrize("viscous", [0, 1], ids=["euler", "laminar"])
-def test_gpu_batch_matches_oracle(viscous, freeze):
+def test_gpu_batch_matches_oracle(viscous, freeze, p_floor):
+    """A few iterations bit-identical to the restatement; the 'floor' case
+    sets the temperature floor above the free stream's p / rho = 1/1.4, so
+    it acts on every cell of every update."""
     from mstcfd import batch
     from mstcfd import meshgen as mg
     cases = _batch_cases(viscous)
     b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
                     implicit=dict(cfl0=40.0, cfl_max=40.0, omega=1.2, autotune=0,
-                                  graph_iters=0, freeze_tol=freeze),
+                                  graph_iters=0, freeze_tol=freeze, p_floor=p_floor),
                     flux=1, order=2, limiter=1, precision=0, viscous=viscous)
     q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
     n_it = 70 if freeze else 12  # the freezing check runs every 50 iterations
@@ -144,7 +148,7 @@ def test_gpu_batch_matches_oracle(viscous, freeze):
         prm = po.params_ext(1, 2, limiter=1, quirks=0, inlet_q=cp["inlet_q"], viscous=viscous,
                             mu=cp["mu"], lam=cp["lambda_"], kappa=cp["kappa"], cv=cp["cv"])
         q, hist = po.lusgs_iterate(om, prm, q0[k], col, n_it, cfl0=40.0, cfl_max=40.0,
-                                   omega=1.2, freeze_tol=freeze)
+                                   omega=1.2, freeze_tol=freeze, p_floor=p_floor)
         assert np.array_equal(got[k], q), k
         assert np.isclose(st["first_l2"][k], hist[0], rtol=1e-12)
         assert np.isclose(st["last_l2"][k], hist[-1], rtol=1e-12)
