@@ -362,9 +362,10 @@ def run_batch(args, ws, rank, grp):
            "warm": None}
     q_cold = b.state()
     conv_cold = conv
+    first_cold = st["first_l2"]
     b.close()
     # the same cold start with the FP32 residual until 1e-3 (then FP64)
-    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1, p_floor=P_FLOOR),
+    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
                      flux=1, order=2, limiter=1, precision=1, viscous=1)
     bm.set_state(q0)
     grp.barrier()
@@ -376,16 +377,16 @@ def run_batch(args, ws, rank, grp):
     out["cold_mixed"] = {"value": round(grp.max(wall_m), 3), "unit": "s",
                          "converged": int(grp.sum((cm >= 0).sum())),
                          "iterations": rm["iterations"],
-                         "precision": "FP32 residual until L2 1e-3, then FP64; FP32 sweeps, FP64 diagonal inversion and update"}
+                         "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update"}
     bm.close()
     if args.warm_train > 0:
-        out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, grp)
+        out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp)
         if out["warm"].get("value"):
             out["warm_speedup"] = round(out["value"] / out["warm"]["value"], 3)
     return out
 
 
-def run_warm(args, fam, cases, q_cold, conv_cold, grp):
+def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     """Learned warm start of the same batch: the network is trained on the
     GPU (tensor-core forward/backward) on ramps of a disjoint seed range
     that the batched solver converged from free stream, then predicts the
@@ -434,15 +435,20 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
     q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
     infer_s = time.perf_counter() - t2
     gemm = _gemm_at_scale(net, feats)
-    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=1e-3, sweep_fp32=1, p_floor=P_FLOOR),
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q_warm)
+    # the same residual tolerance as the cold start: L2 <= tol x the cold
+    # run's first-iteration L2 of each case (an absolute target, not one
+    # relative to the warm field's smaller initial residual)
+    b.set_l2_ref(first_cold)
     t3 = time.perf_counter()
     r = b.solve()
     solve_s = time.perf_counter() - t3
     grp.barrier()
     wall = grp.max(infer_s + solve_s)
-    conv = b.case_status()["conv_iter"]
+    stw = b.case_status()
+    conv = stw["conv_iter"]
     qw = b.state()
     b.close()
     net.close()
@@ -454,7 +460,9 @@ def run_warm(args, fam, cases, q_cold, conv_cold, grp):
     it_w = [int(conv[k]) for k in both]
     it_c = [int(conv_cold[k]) for k in both]
     return {"value": round(wall, 3), "unit": "s", "inference_s": round(infer_s, 3),
-            "precision": "FP32 residual until L2 1e-3, then FP64; FP32 sweeps, FP64 diagonal inversion and update",
+            "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update",
+            "tolerance": "L2 <= 1e-8 x the cold start's first-iteration L2 of each case "
+                         "(the same absolute residual as the cold start)",
             "converged": int(grp.sum((conv >= 0).sum())), "iterations": r["iterations"],
             "median_case_iterations": int(np.median(conv[conv >= 0])) if (conv >= 0).any() else None,
             "median_case_iterations_cold": int(np.median(conv_cold[conv_cold >= 0]))
@@ -603,6 +611,8 @@ def main():
     ap.add_argument("--warm-train", type=int, default=32,
                     help="training cases of the learned warm start (0: no warm start)")
     ap.add_argument("--warm-steps", type=int, default=400)
+    ap.add_argument("--fp32-until", type=float, default=1e-3,
+                    help="the batch's production runs use the FP32 residual until this L2")
     ap.add_argument("--tgv-n", type=int, default=128,
                     help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
     ap.add_argument("--tgv-steps", type=int, default=10)

@@ -419,6 +419,12 @@ mst_status mst_batch_colors(const mst_batch *b, int *color);
 /* States of all cases, cases in order, rows of 4 doubles; setting the
  * state restarts the convergence bookkeeping. */
 mst_status mst_batch_set_state(mst_batch *b, const double *q);
+/* Reference L2 per case [n_cases] (after mst_batch_set_state, which clears
+ * it): the tolerance, the SER CFL and limiter freezing then measure L2
+ * against it instead of the first iteration's L2 -- e.g. a warm-started
+ * solve held to the same absolute residual as the cold start it is
+ * compared with.  NULL clears it. */
+mst_status mst_batch_set_l2_ref(mst_batch *b, const double *l2_ref);
 mst_status mst_batch_get_state(mst_batch *b, double *q);
 /* Exactly n iterations (no convergence stop, no graph). */
 mst_status mst_batch_iterate(mst_batch *b, int n);

@@ -80,6 +80,7 @@ struct mst_batch {
   double* diag = nullptr;
   float4* dqf = nullptr;         // FP32 sweeps: dQ* / dQ in FP32
   bool sweep32 = false;
+  bool first_fixed = false;      // reference L2s set by mst_batch_set_l2_ref
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
   // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
   // lo is set, FP64 afterwards; the sweeps are FP64 throughout
@@ -227,6 +228,7 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
   na.l2_win = b->l2_win;
   na.freeze_tol = b->ip.freeze_tol;
+  na.first_fixed = b->first_fixed ? 1 : 0;
   na.cfl0 = b->ip.cfl0;
   na.cfl_max = b->ip.cfl_max;
   na.tol = b->ip.tol;
@@ -496,6 +498,15 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   b->cur = 0;
   // a new solve starts in the FP32-residual phase when one is configured
   b->lo = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
+  if (b->first_fixed) {
+    // graphs captured with caller-set reference L2s: rebuild them
+    for (int i = 0; i < 2; ++i)
+      if (b->graph[i]) {
+        cudaGraphExecDestroy(b->graph[i]);
+        b->graph[i] = nullptr;
+      }
+  }
+  b->first_fixed = false;
   b->lo_below = 0;
   b->lo_since = 0;
   if (b->lo || b->sweep32) {
@@ -506,6 +517,26 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   st = reset_progress(b);
   if (st) return st;
   B_CU(cudaStreamSynchronize(b->ctx->stream));
+  return MST_OK;
+}
+
+mst_status mst_batch_set_l2_ref(mst_batch* b, const double* l2_ref) {
+  if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
+  if (!l2_ref) {
+    b->first_fixed = false;
+  } else {
+    for (int i = 0; i < b->n_cases; ++i)
+      if (!(l2_ref[i] > 0.0))
+        return mst_internal_fail(MST_EINVAL, "reference L2 values must be > 0");
+    B_CU(cudaMemcpy(b->first, l2_ref, sizeof(double) * b->n_cases, cudaMemcpyHostToDevice));
+    b->first_fixed = true;
+  }
+  // the captured graphs hold the norm arguments: rebuild them
+  for (int i = 0; i < 2; ++i)
+    if (b->graph[i]) {
+      cudaGraphExecDestroy(b->graph[i]);
+      b->graph[i] = nullptr;
+    }
   return MST_OK;
 }
 

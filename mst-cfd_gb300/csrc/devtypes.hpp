@@ -173,6 +173,7 @@ struct CaseNormArgs {
   int* frozen;             // [n_cases] limiter-freezing state (or nullptr)
   double* l2_win;          // [n_cases] L2 at the last freezing-window check
   double cfl0, cfl_max, tol, freeze_tol;
+  int first_fixed;         // first[] holds reference L2s set by the caller
 };
 
 // Precisions / schemes (mirrors of the public enums)

@@ -70,6 +70,15 @@ class Batch:
         q = capi.f64(np.concatenate(states, 0), (int(self.case_cells[-1]), 4))
         capi.check(capi.load().mst_batch_set_state(self._h, capi.dptr(q)))
 
+    def set_l2_ref(self, l2_ref):
+        """Per-case reference L2 of the tolerance (after set_state); None
+        clears it (the first iteration's L2 is the reference again)."""
+        if l2_ref is None:
+            capi.check(capi.load().mst_batch_set_l2_ref(self._h, None))
+            return
+        r = capi.f64(np.asarray(l2_ref, np.float64), (len(self.meshes),))
+        capi.check(capi.load().mst_batch_set_l2_ref(self._h, capi.dptr(r)))
+
     def state(self):
         q = np.zeros((int(self.case_cells[-1]), 4))
         capi.check(capi.load().mst_batch_get_state(self._h, capi.dptr(q)))

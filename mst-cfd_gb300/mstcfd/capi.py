@@ -188,6 +188,7 @@ def load():
         "mst_batch_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
         "mst_batch_colors": (C.c_int, [C.c_void_p, _ip]),
         "mst_batch_set_state": (C.c_int, [C.c_void_p, _dp]),
+        "mst_batch_set_l2_ref": (C.c_int, [C.c_void_p, _dp]),
         "mst_batch_get_state": (C.c_int, [C.c_void_p, _dp]),
         "mst_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
         "mst_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(BatchResult)]),

@@ -284,3 +284,36 @@ def test_gpu_batch_fp32_sweeps_reach_tolerance(fp32_until):
     for a, c in zip(out[0], out[1]):
         rms = np.sqrt(np.mean((a - c) ** 2)) / np.sqrt(np.mean(a ** 2))
         assert rms < 1e-3
+
+
+@pytest.mark.gpu
+def test_gpu_batch_reference_l2_sets_the_tolerance():
+    """With a caller-set reference L2 the tolerance, SER CFL and freezing
+    measure against it: a reference equal to the first-iteration L2 gives
+    the plain solve bit-for-bit; with a 10x larger one every case meets the
+    correspondingly looser absolute target."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    imp = dict(max_iter=3000, graph_iters=10)
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    b.set_state(q0)
+    b.solve()
+    st = b.case_status()
+    q_plain = b.state()
+    b.set_state(q0)
+    b.set_l2_ref(st["first_l2"])
+    b.solve()
+    st2 = b.case_status()
+    assert np.array_equal(st2["conv_iter"], st["conv_iter"])
+    for a, c in zip(b.state(), q_plain):
+        assert np.array_equal(a, c)
+    b.set_state(q0)
+    b.set_l2_ref(10.0 * st["first_l2"])
+    b.solve()
+    st3 = b.case_status()
+    assert np.all(st3["conv_iter"] >= 0)
+    assert np.all(st3["last_l2"] <= 1e-8 * 10.0 * st["first_l2"] * 1.0001)
+    b.close()
