@@ -368,8 +368,8 @@ typedef struct mst_implicit_params {
   /* mixed precision (FP64 production path only): a solve starts with the
    * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
    * state) and switches to the FP64 residual once every unconverged case
-   * is below fp32_until * L2_first (or, with at least half of them below,
-   * when no further case has crossed it for 1000 iterations); 0: FP64
+   * is below fp32_until * L2_first or stagnating in FP32 (its L2 has not
+   * fallen by 10% for 500 iterations: the FP32 residual's floor); 0: FP64
    * residual throughout */
   double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */

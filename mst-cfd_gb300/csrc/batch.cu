@@ -86,7 +86,9 @@ struct mst_batch {
   // lo is set, FP64 afterwards; the sweeps are FP64 throughout
   bool lo = false;
   void* grad32 = nullptr;
-  int lo_below = 0, lo_since = 0;  // phase-switch bookkeeping
+  // phase-switch bookkeeping: per case the best FP32-phase L2 and when
+  std::vector<double> lo_best;
+  std::vector<int> lo_best_it;
   bool tuned = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [FP64 phase, FP32 phase]
   int graph_iters[2] = {0, 0};
@@ -507,8 +509,8 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
       }
   }
   b->first_fixed = false;
-  b->lo_below = 0;
-  b->lo_since = 0;
+  b->lo_best.clear();
+  b->lo_best_it.clear();
   if (b->lo || b->sweep32) {
     cudaError_t e = mst::fast::launch_to_f32(b->ctx->q_old, b->ctx->qf_old, b->ctx->dm.n_cells,
                                              b->ctx->stream);
@@ -605,19 +607,29 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     done = h[1];
     if (done >= b->n_cases) break;
     if (b->lo) {
-      // leave the FP32 phase once every unconverged case is below
-      // fp32_until, or when no further case has crossed it for 1000
-      // iterations while at least half of them have
+      // leave the FP32 phase once every case is converged, below
+      // fp32_until, or stagnating in FP32 (its L2 has not fallen by 10%
+      // for 500 iterations: the FP32 residual's floor)
       B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
-      int below = 0;
-      for (int i = 0; i < b->n_cases; ++i) below += (l[i] <= b->ip.fp32_until * f[i]) ? 1 : 0;
-      if (below > b->lo_below) {
-        b->lo_below = below;
-        b->lo_since = iters;
+      B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
+      if (b->lo_best.size() != (size_t)b->n_cases) {
+        b->lo_best.assign(b->n_cases, 1e300);
+        b->lo_best_it.assign(b->n_cases, iters);
       }
-      if (below == b->n_cases ||
-          (2 * below >= b->n_cases && iters - b->lo_since >= 1000)) {
+      int ready = 0;
+      for (int i = 0; i < b->n_cases; ++i) {
+        if (cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i]) {
+          ++ready;
+          continue;
+        }
+        if (l[i] < 0.9 * b->lo_best[i]) {
+          b->lo_best[i] = l[i];
+          b->lo_best_it[i] = iters;
+        }
+        if (iters - b->lo_best_it[i] >= 500) ++ready;
+      }
+      if (ready == b->n_cases) {
         b->lo = false;
         st = ensure_graph();
         if (st) return st;
