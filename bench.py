@@ -195,8 +195,7 @@ def _gemm_at_scale(net, feats):
             "tflops": round(tflops, 2), "tensor_frac": round(tflops / tf_peak, 4),
             "tensor_peak": tf_peak, "tensor_peak_source": tf_src,
             "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4), "hbm_peak_source": hbm_src,
-            "flops_per_byte": round(g["flops"] / g["bytes"], 1),
-            "ridge_flops_per_byte": round(ridge, 1),
+            "flops_per_byte": round(g["flops"] / g["bytes"], 1), "ridge_flops_per_byte": round(ridge, 1),
             "bound": "hbm" if g["flops"] / g["bytes"] < ridge else "tensor"}
 
 
@@ -311,18 +310,6 @@ def _wedge_cases(n_cases, lo, hi):
 P_FLOOR = 0.01
 
 
-def _production(args):
-    """Implicit parameters of the batch's production runs (warm start and
-    the matching cold start)."""
-    return dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1,
-                p_floor=P_FLOOR)
-
-
-def _production_label(args):
-    return (f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 "
-            f"diagonal inversion and update")
-
-
 def run_batch(args, ws, rank, grp):
     """Cold-start batched LU-SGS solve of the wedge family to L2 1e-8.  With
     N ranks the cases are split by greedy size balancing, each rank solves
@@ -378,7 +365,7 @@ def run_batch(args, ws, rank, grp):
     first_cold = st["first_l2"]
     b.close()
     # the same cold start with the FP32 residual until 1e-3 (then FP64)
-    bm = batch.Batch(cases, implicit=_production(args),
+    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
                      flux=1, order=2, limiter=1, precision=1, viscous=1)
     bm.set_state(q0)
     grp.barrier()
@@ -390,7 +377,7 @@ def run_batch(args, ws, rank, grp):
     out["cold_mixed"] = {"value": round(grp.max(wall_m), 3), "unit": "s",
                          "converged": int(grp.sum((cm >= 0).sum())),
                          "iterations": rm["iterations"],
-                         "precision": _production_label(args)}
+                         "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update"}
     bm.close()
     if args.warm_train > 0:
         out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp)
@@ -448,7 +435,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
     infer_s = time.perf_counter() - t2
     gemm = _gemm_at_scale(net, feats)
-    b = batch.Batch(cases, implicit=_production(args),
+    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q_warm)
     # the same residual tolerance as the cold start: L2 <= tol x the cold
@@ -473,7 +460,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     it_w = [int(conv[k]) for k in both]
     it_c = [int(conv_cold[k]) for k in both]
     return {"value": round(wall, 3), "unit": "s", "inference_s": round(infer_s, 3),
-            "precision": _production_label(args),
+            "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update",
             "tolerance": "L2 <= 1e-8 x the cold start's first-iteration L2 of each case "
                          "(the same absolute residual as the cold start)",
             "converged": int(grp.sum((conv >= 0).sum())), "iterations": r["iterations"],

@@ -365,12 +365,12 @@ typedef struct mst_implicit_params {
    * dropped) until density and pressure stay above a fifth of their
    * current values. */
   double freeze_tol;
-  /* mixed precision (FP64 production path only): every case starts with
-   * the FP32 residual (FP32 gradient, reconstruction and flux; FP64 state)
-   * and switches, on its own, to the FP64 residual once it is below
-   * fp32_until * L2_first or stagnating in FP32 (its L2 has not fallen by
-   * 10% for 500 iterations: the FP32 residual's floor); convergence is
-   * always judged on the FP64 residual.  0: FP64 residual throughout */
+  /* mixed precision (FP64 production path only): a solve starts with the
+   * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
+   * state) and switches to the FP64 residual once every unconverged case
+   * is below fp32_until * L2_first or stagnating in FP32 (its L2 has not
+   * fallen by 10% for 500 iterations: the FP32 residual's floor); 0: FP64
+   * residual throughout */
   double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */

@@ -82,14 +82,9 @@ struct mst_batch {
   bool sweep32 = false;
   bool first_fixed = false;      // reference L2s set by mst_batch_set_l2_ref
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
-  // mixed precision: while lo is set, every iteration runs the FP32
-  // residual (FP32 state copy and gradient) for the cases still in their
-  // FP32 phase (case_lo[k] = 1) and the FP64 residual for the others; each
-  // case leaves its FP32 phase on its own
+  // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
+  // lo is set, FP64 afterwards; the sweeps are FP64 throughout
   bool lo = false;
-  bool mixed = false;            // fp32_until set: FP32 state copy kept
-  int* case_lo = nullptr;
-  std::vector<int> lo_host;
   void* grad32 = nullptr;
   // phase-switch bookkeeping: per case the best FP32-phase L2 and when
   std::vector<double> lo_best;
@@ -121,28 +116,27 @@ mst_status bupload(mst_batch* b, T** p, const std::vector<T>& v) {
 double4_32a* qbuf(mst_batch* b, int which) { return which ? b->ctx->q_new : b->ctx->q_old; }
 // FP32 copy of the state, kept where an FP32 residual reads it
 float4* qfbuf(mst_batch* b, int which) {
-  if (b->ctx->p.precision != MST_PREC_FP32 && !b->mixed && !b->sweep32) return nullptr;
+  if (b->ctx->p.precision != MST_PREC_FP32 && !b->lo && !b->sweep32) return nullptr;
   return which ? b->ctx->qf_new : b->ctx->qf_old;
 }
 
 bool exact(const mst_batch* b) { return b->ctx->p.precision == MST_PREC_FP64_EXACT; }
 
-// one residual pass into ctx->r: FP32 (f32) or the context's precision,
-// over the cells dm does not skip
-mst_status residual_pass(mst_batch* b, int which, bool f32, const mst::DevMesh& dm) {
+// the residual R(Q) of the current state into ctx->r
+mst_status enqueue_residual(mst_batch* b, int which) {
   mst_ctx* c = b->ctx;
-  const int prec = f32 ? MST_PREC_FP32 : c->p.precision;
-  void* grad = f32 ? b->grad32 : c->grad;
+  const int prec = b->lo ? MST_PREC_FP32 : c->p.precision;
+  void* grad = b->lo ? b->grad32 : c->grad;
   cudaStream_t s = c->stream;
   const double4_32a* q = qbuf(b, which);
   const float4* qf = qfbuf(b, which);
   cudaError_t e = cudaSuccess;
   if (c->p.order == 2) {
-    if (exact(b) && !f32) e = mst::exact::launch_gradient(prec, dm, q, grad, 0, s);
+    if (exact(b) && !b->lo) e = mst::exact::launch_gradient(prec, c->dm, q, grad, 0, s);
     else if (qf)
-      e = mst::fast::launch_gradient_dt(prec, dm, q, qf, grad, 0, 0.0, nullptr, nullptr,
+      e = mst::fast::launch_gradient_dt(prec, c->dm, q, qf, grad, 0, 0.0, nullptr, nullptr,
                                         nullptr, s);
-    else e = mst::fast::launch_gradient(prec, dm, q, grad, 0, s);
+    else e = mst::fast::launch_gradient(prec, c->dm, q, grad, 0, s);
     if (e != cudaSuccess)
       return mst_internal_fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
   }
@@ -156,30 +150,16 @@ mst_status residual_pass(mst_batch* b, int which, bool f32, const mst::DevMesh& 
   mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa, c->p.cv);
   a.case_tab = b->case_tab;
   a.case_tab_f = b->case_tab_f;
-  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE && !f32) {
+  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE && !b->lo) {
     a.case_frozen = b->frozen;
     a.phi = b->phi;
   }
-  e = (exact(b) && !f32) ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, dm, a, 0, s)
-                         : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, dm, a, 0, s);
+  e = (exact(b) && !b->lo)
+          ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
+          : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
   if (e != cudaSuccess)
     return mst_internal_fail(MST_ECUDA, std::string("residual: ") + cudaGetErrorString(e));
   return MST_OK;
-}
-
-// the residual R(Q) of the current state into ctx->r: in the mixed phase
-// an FP32 pass over the cases in their FP32 phase and an FP64 pass over
-// the others (each skips the other's cases)
-mst_status enqueue_residual(mst_batch* b, int which) {
-  if (!b->lo) return residual_pass(b, which, false, b->ctx->dm);
-  mst::DevMesh d32 = b->ctx->dm;
-  d32.case_lo = b->case_lo;
-  d32.lo_want = 1;
-  mst::DevMesh d64 = d32;
-  d64.lo_want = 0;
-  mst_status st = residual_pass(b, which, true, d32);
-  if (st) return st;
-  return residual_pass(b, which, false, d64);
 }
 
 mst::LusgsArgs sweep_args(mst_batch* b, int which) {
@@ -246,9 +226,8 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.conv_iter = b->conv_iter;
   na.n_conv = b->n_conv;
   na.iter = b->iter;
-  // the limiter-freezing state machine runs for cases in their FP64 phase
-  na.frozen = b->ip.freeze_tol > 0 ? b->frozen : nullptr;
-  na.case_lo = b->lo ? b->case_lo : nullptr;
+  // the limiter-freezing state machine runs in the FP64 phase only
+  na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
   na.l2_win = b->l2_win;
   na.freeze_tol = b->ip.freeze_tol;
   na.first_fixed = b->first_fixed ? 1 : 0;
@@ -468,7 +447,6 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->dqf, b->sweep32 ? sizeof(float4) * (size_t)nC : 0)) ||
-      (st = balloc(b.get(), &b->case_lo, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
                                             ? sizeof(float) * 8 * (size_t)nC : 0)) ||
       (st = reset_progress(b.get()))) {
@@ -521,11 +499,7 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   if (st) return st;
   b->cur = 0;
   // a new solve starts in the FP32-residual phase when one is configured
-  b->mixed = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
-  b->lo = b->mixed;
-  b->lo_host.assign(b->n_cases, b->lo ? 1 : 0);
-  B_CU(cudaMemcpy(b->case_lo, b->lo_host.data(), sizeof(int) * b->n_cases,
-                  cudaMemcpyHostToDevice));
+  b->lo = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
   if (b->first_fixed) {
     // graphs captured with caller-set reference L2s: rebuild them
     for (int i = 0; i < 2; ++i)
@@ -633,9 +607,9 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     done = h[1];
     if (done >= b->n_cases) break;
     if (b->lo) {
-      // each case leaves its FP32 phase once converged, below fp32_until,
-      // or stagnating in FP32 (its L2 has not fallen by 10% for 500
-      // iterations: the FP32 residual's floor)
+      // leave the FP32 phase once every case is converged, below
+      // fp32_until, or stagnating in FP32 (its L2 has not fallen by 10%
+      // for 500 iterations: the FP32 residual's floor)
       B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
@@ -643,29 +617,19 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
         b->lo_best.assign(b->n_cases, 1e300);
         b->lo_best_it.assign(b->n_cases, iters);
       }
-      bool changed = false;
-      int n_lo = 0;
+      int ready = 0;
       for (int i = 0; i < b->n_cases; ++i) {
-        if (!b->lo_host[i]) continue;
-        bool ready = cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i];
-        if (!ready) {
-          if (l[i] < 0.9 * b->lo_best[i]) {
-            b->lo_best[i] = l[i];
-            b->lo_best_it[i] = iters;
-          }
-          ready = iters - b->lo_best_it[i] >= 500;
+        if (cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i]) {
+          ++ready;
+          continue;
         }
-        if (ready) {
-          b->lo_host[i] = 0;
-          changed = true;
-        } else {
-          ++n_lo;
+        if (l[i] < 0.9 * b->lo_best[i]) {
+          b->lo_best[i] = l[i];
+          b->lo_best_it[i] = iters;
         }
+        if (iters - b->lo_best_it[i] >= 500) ++ready;
       }
-      if (changed)
-        B_CU(cudaMemcpy(b->case_lo, b->lo_host.data(), sizeof(int) * b->n_cases,
-                        cudaMemcpyHostToDevice));
-      if (n_lo == 0) {
+      if (ready == b->n_cases) {
         b->lo = false;
         st = ensure_graph();
         if (st) return st;

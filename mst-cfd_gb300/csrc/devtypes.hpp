@@ -44,30 +44,19 @@ struct DevMesh {
   // iteration that converged them both state buffers hold the same state.
   const int* c_case;
   const int* case_conv;
-  // mixed-precision batches: the phase of every case (1: FP32 residual,
-  // 0: FP64) and the phase a launch computes; cells of cases in the other
-  // phase are skipped like converged ones (nullptr: one phase)
-  const int* case_lo;
-  int lo_want;
 };
 
-// true when case k needs nothing from this launch: converged, or in the
-// other precision phase
-__device__ __forceinline__ bool case_skipped(const DevMesh& m, int k) {
-  return m.case_conv[k] >= 0 || (m.case_lo && m.case_lo[k] != m.lo_want);
-}
-
-// true when device cell c belongs to a case this launch skips
+// true when device cell c belongs to a converged case of a batch
 __device__ __forceinline__ bool cell_case_done(const DevMesh& m, int c) {
-  return m.case_conv && case_skipped(m, m.c_case[c]);
+  return m.case_conv && m.case_conv[m.c_case[c]] >= 0;
 }
 
-// true when every cell of [c0, c1) belongs to a skipped case (the cases
+// true when every cell of [c0, c1) belongs to a converged case (the cases
 // are contiguous ranges of device cells)
 __device__ __forceinline__ bool range_cases_done(const DevMesh& m, int c0, int c1) {
   if (!m.case_conv || c1 <= c0) return false;
   for (int k = m.c_case[c0], e = m.c_case[c1 - 1]; k <= e; ++k)
-    if (!case_skipped(m, k)) return false;
+    if (m.case_conv[k] < 0) return false;
   return true;
 }
 
@@ -185,7 +174,6 @@ struct CaseNormArgs {
   double* l2_win;          // [n_cases] L2 at the last freezing-window check
   double cfl0, cfl_max, tol, freeze_tol;
   int first_fixed;         // first[] holds reference L2s set by the caller
-  const int* case_lo;      // [n_cases] 1 while in the FP32 phase (no freezing), or nullptr
 };
 
 // Precisions / schemes (mirrors of the public enums)
