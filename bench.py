@@ -611,7 +611,7 @@ def main():
     ap.add_argument("--warm-train", type=int, default=32,
                     help="training cases of the learned warm start (0: no warm start)")
     ap.add_argument("--warm-steps", type=int, default=400)
-    ap.add_argument("--fp32-until", type=float, default=1e-3,
+    ap.add_argument("--fp32-until", type=float, default=1e-5,
                     help="the batch's production runs use the FP32 residual until this L2")
     ap.add_argument("--tgv-n", type=int, default=128,
                     help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
