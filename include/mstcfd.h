@@ -226,7 +226,9 @@ mst_status mst_ctx3d_residual(mst_ctx3d *c, double *r);
 mst_status mst_ctx3d_gradient(mst_ctx3d *c, double *g);
 /* nsteps RK2 steps at the global CFL step, the state kept in HBM; t_end >
  * 0 cuts the last step to reach it.  Simulated time through *time
- * (nullable).  mst_ctx3d_last_timing: device milliseconds and kernel
+ * (nullable).  MST_EDIVERGED when a step before t_end had zero length
+ * (some cell's CFL step was not positive: NaN or non-positive density or
+ * pressure).  mst_ctx3d_last_timing: device milliseconds and kernel
  * launches of the last mst_ctx3d_step. */
 mst_status mst_ctx3d_step(mst_ctx3d *c, int nsteps, double t_end, double *time);
 mst_status mst_ctx3d_last_timing(mst_ctx3d *c, double *ms, int *launches);
@@ -319,7 +321,9 @@ mst_status mst_solve_device_noalloc(mst_ctx *c, const double *q_dev,
 /* Device-resident time stepping: nsteps steps of the configured scheme
  * without host round trips (the Work::work loop, work/Work.cpp:53-89, with
  * the state kept in HBM).  t_end > 0 clips the last step to reach t_end
- * exactly.  last (nullable) receives the norms of the final step. */
+ * exactly.  last (nullable) receives the norms of the final step.
+ * Returns MST_EDIVERGED when the final step's residual or mass is not
+ * finite (the state left the physical range). */
 mst_status mst_step(mst_ctx *c, int nsteps, double t_end, mst_norms *last);
 
 /* Simulated time of the context (sum of the steps taken). */

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -696,6 +697,7 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
       CU(up(&d.f_eta32, fe32));
     }
     CU(up(&d.c_vol, L.c_vol));
+    for (double v : L.c_vol) c->volumes_ok = c->volumes_ok && std::isfinite(v) && v > 0.0;
     std::vector<double> ivol(L.c_vol.size());
     for (size_t i = 0; i < ivol.size(); ++i) ivol[i] = 1.0 / L.c_vol[i];
     CU(up(&d.c_ivol, ivol));
@@ -1011,8 +1013,23 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
   c->timed = true;
   c->grad_valid = false;
   drain_profile(c);
-  if (last) return read_norms(c, last);
-  CU(cudaStreamSynchronize(c->stream));
+  if (nsteps == 0) {
+    if (last) return read_norms(c, last);
+    CU(cudaStreamSynchronize(c->stream));
+    return MST_OK;
+  }
+  // the last step's norms: on a mesh of finite positive volumes, a
+  // residual or mass that is not finite means the state left the physical
+  // range (NaN, non-positive density or pressure)
+  mst_norms n{};
+  mst_status st = read_norms(c, &n);
+  if (st) return st;
+  if (last) *last = n;
+  bool finite = std::isfinite(n.mass);
+  for (int j = 0; j < 4; ++j) finite = finite && std::isfinite(n.l2_resid[j]);
+  if (!finite && c->volumes_ok)
+    return fail(MST_EDIVERGED, "mst_step: the residual or the mass is not finite (NaN or "
+                               "non-positive density or pressure)");
   return MST_OK;
 }
 

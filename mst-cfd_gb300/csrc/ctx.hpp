@@ -78,6 +78,10 @@ struct mst_ctx {
   std::vector<double> kms;
   bool timed = false;
   bool grad_valid = false;
+  // every cell volume finite and positive: only then does a non-finite
+  // residual mean divergence (the reference's own geometry gives NaN
+  // volumes on degenerate quads, and its results carry them)
+  bool volumes_ok = true;
   std::vector<void*> allocs;
   mst_node_avg* node_avg = nullptr;
 };

@@ -504,7 +504,14 @@ mst_status mst_ctx3d_step(mst_ctx3d* c, int nsteps, double t_end, double* time) 
   C3(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->last_ms = ms;
   drain3(c);
-  if (time) C3(cudaMemcpy(time, c->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
+  double sc[2] = {0.0, 0.0};
+  C3(cudaMemcpy(sc, c->scal, sizeof sc, cudaMemcpyDeviceToHost));
+  if (time) *time = sc[1];
+  // a step of zero length before t_end: the CFL step of some cell was not
+  // positive (NaN, non-positive density or pressure)
+  if (nsteps > 0 && !(sc[0] > 0.0) && !(t_end > 0.0 && sc[1] >= t_end))
+    return fail3(MST_EDIVERGED, "mst_ctx3d_step: non-positive CFL step (NaN or non-positive "
+                                "density or pressure)");
   return MST_OK;
 }
 

@@ -178,3 +178,28 @@ def test_conservation_periodic(prec):
     before = (V * q0).sum(0)
     after = (V * s.state()).sum(0)
     assert np.all(np.abs(after - before) <= 1e-11 * np.abs(before).max())
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_step_reports_divergence(prec):
+    """A state that leaves the physical range (here one cell of negative
+    pressure) makes mst_step return MST_EDIVERGED instead of stepping on
+    silently with NaN; a physical state on the same context still steps."""
+    from mstcfd import Solver, capi
+    from mstcfd import meshgen as mg
+    m = _periodic(16)
+    mesh, om = _both(m)
+    q0 = mg.isentropic_vortex(om.cell_ctr)
+    s = Solver(mesh, flux=0, order=2, limiter=2, reference_quirks=0, precision=prec,
+               time_scheme=1, dt_mode=1, cfl=0.5)
+    s.set_state(q0)
+    s.step(2)
+    bad = q0.copy()
+    bad[5, 3] = 0.1 * 0.5 * (bad[5, 1] ** 2 + bad[5, 2] ** 2) / bad[5, 0]  # E < kinetic: p < 0
+    s.set_state(bad)
+    with pytest.raises(capi.MstError) as e:
+        s.step(3)
+    assert e.value.status == capi.EDIVERGED
+    s.set_state(q0)
+    s.step(2)
+    s.close()

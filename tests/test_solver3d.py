@@ -256,3 +256,22 @@ def test_gpu3d_tgv_kinetic_energy_decays_fp32_tracks_fp64():
     for h in hist.values():
         assert np.all(np.diff(h) < 0)
     assert np.abs(hist[2] - hist[1]).max() <= 1e-4 * hist[1][0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 2])
+def test_gpu3d_step_reports_divergence(prec):
+    from mstcfd import capi
+    from mstcfd import meshgen as mg
+    m = _tgv_mesh(3)
+    q0 = mg.taylor_green(m["cell_centroid"], mach=0.3)
+    s = _solver(m, precision=prec, order=2, limiter=3)
+    s.set_state(q0)
+    s.step(1)
+    bad = q0.copy()
+    bad[7, 4] = 0.0  # E = 0 < kinetic energy: negative pressure
+    s.set_state(bad)
+    with pytest.raises(capi.MstError) as e:
+        s.step(2)
+    assert e.value.status == capi.EDIVERGED
+    s.close()
