@@ -503,6 +503,41 @@ def run_cpu_sample(m, steps, budget_s=30.0):
     return 2.0 * m["n_cells"] * done / t_total / 1e6, cores, done, t_total
 
 
+def run_batch_scale(args, grp):
+    """Throughput of the batched LU-SGS at a larger batch (a fixed number
+    of iterations, FP64 residual and sweeps, no convergence target): the
+    Mcell-iterations/s the cold-start path sustains at config-4 scale."""
+    from mstcfd import Mesh, batch
+    from mstcfd import meshgen as mg
+    gamma, cv = 1.4, 1.0 / (1.4 * 0.4)
+    t0 = time.perf_counter()
+    fam = _wedge_cases(args.scale_cases, args.scale_cells[0], args.scale_cells[1])
+    cases, q0 = [], []
+    for m, mach, angle, re in fam:
+        mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                                m["n_cells"])
+        mu = mach / re
+        cases.append((mesh, batch.case_params(mg.freestream(mach), mu=mu, lambda_=-2 / 3 * mu,
+                                              kappa=mu * gamma * cv / 0.72, cv=cv)))
+        q0.append(mg.freestream(mach, mesh.n_cells))
+    setup_s = time.perf_counter() - t0
+    b = batch.Batch(cases, implicit=dict(max_iter=args.scale_iters, p_floor=P_FLOOR,
+                                         tol=1e-30),
+                    flux=1, order=2, limiter=1, precision=1, viscous=1)
+    b.set_state(q0)
+    grp.barrier()
+    r = b.solve()
+    cells = int(sum(m.n_cells for m, _ in cases))
+    info = b.info()
+    b.close()
+    return {"cases": args.scale_cases, "cells": cells, "cell_range": list(args.scale_cells),
+            "iterations": r["iterations"], "device_s": round(r["ms"] * 1e-3, 3),
+            "Mcell_iterations_per_s": round(cells * r["iterations"] / (r["ms"] * 1e-3) / 1e6, 1),
+            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
+            "mesh_setup_s": round(setup_s, 1),
+            "precision": "FP64 residual and sweeps (the cold-start path)"}
+
+
 def run_tgv3d(args, grp):
     """3D Taylor-Green vortex (Ma 0.1, Re 1600, laminar) on the periodic
     jittered Kuhn tetrahedral mesh of (tgv_n)^3 x 6 cells: FP32 and FP64
@@ -613,6 +648,10 @@ def main():
     ap.add_argument("--warm-steps", type=int, default=400)
     ap.add_argument("--fp32-until", type=float, default=1e-5,
                     help="the batch's production runs use the FP32 residual until this L2")
+    ap.add_argument("--scale-cases", type=int, default=0,
+                    help="cases of the batch-throughput line at scale (0: skip)")
+    ap.add_argument("--scale-cells", type=int, nargs=2, default=[20000, 400000])
+    ap.add_argument("--scale-iters", type=int, default=200)
     ap.add_argument("--tgv-n", type=int, default=128,
                     help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
     ap.add_argument("--tgv-steps", type=int, default=10)
@@ -652,6 +691,7 @@ def main():
     results, roof, nC = run_gpu(args, ws, rank, local, grp)
     batch_line = run_batch(args, ws, rank, grp) if args.batch_cases > 0 else None
     tgv_line = run_tgv3d(args, grp) if args.tgv_n > 0 else None
+    scale_line = run_batch_scale(args, grp) if args.scale_cases > 0 else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         m = _workload(args.n)
@@ -674,6 +714,8 @@ def main():
             "gpu_launches": fp32["launches"],
             "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks"),
             "batch": batch_line, "tgv3d": tgv_line}
+    if scale_line:
+        line["batch_scale"] = scale_line
     print(json.dumps(line))
 
 
