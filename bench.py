@@ -353,7 +353,8 @@ def run_batch(args, ws, rank, grp):
            "Mcell_iterations_per_s": round(cells * r["iterations"] / (r["ms"] * 1e-3) / 1e6, 1),
            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
            "graph_iters": info["graph_iters"],
-           "workload": (f"{len(cases)} compression ramps, {args.batch_cells[0]}-"
+           "workload": (f"{len(cases)} compression ramps (no-slip flat plate and ramp), "
+                        f"{args.batch_cells[0]}-"
                         f"{args.batch_cells[1]} triangles each, Mach U[1.5,3], angle U[5,15] deg "
                         f"(attached shocks), "
                         f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, temperature floor p >= "

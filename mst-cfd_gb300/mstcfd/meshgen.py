@@ -183,12 +183,20 @@ def tri_box(nx=40, ny=20, lx=4.0, ly=2.0, jitter=0.2, seed=1,
 
 
 def wedge(cells=20000, angle_deg=10.0, seed=1, length=3.0, height=1.5, ramp_x=0.5,
-          jitter=0.2):
+          jitter=0.2, upstream=WALL):
     """Supersonic compression ramp: the box [0,length]x[0,height] whose floor
     turns up by angle_deg at x = ramp_x, triangulated with about `cells`
     jittered Delaunay triangles (the triangulation of the box, mapped so
     the floor follows the ramp).  Zones: inlet (left), outlet (right and
-    top), symmetry (floor before the ramp), wall (the ramp)."""
+    top), the floor before the ramp (`upstream`), wall (the ramp).
+
+    upstream = WALL (default): a flat plate from the inlet, so the laminar
+    boundary layer develops ahead of the ramp (the classic compression-ramp
+    interaction).  SYMMETRY: a slip floor; the boundary layer then starts at
+    the ramp corner, and in the laminar cases the slip/no-slip junction
+    drives the corner cell towards vacuum (a state the implicit update can
+    only leave through the temperature floor, after which its case stalls).
+    For inviscid cases both give the same (mirror) boundary."""
     ny = max(4, int(round(np.sqrt(cells * height / (2.0 * length)))))
     nx = max(4, int(round(cells / (2.0 * ny))))
     pts, tri, en, c0, c1, interior, side, mid = _box_triangulation(nx, ny, length, height,
@@ -200,7 +208,7 @@ def wedge(cells=20000, angle_deg=10.0, seed=1, length=3.0, height=1.5, ramp_x=0.
     floor = side == 2
     groups = [(np.where(interior)[0], INTERIOR),
               (np.where(side == 0)[0], INLET),
-              (np.where(floor & (mid[:, 0] < ramp_x))[0], SYMMETRY),
+              (np.where(floor & (mid[:, 0] < ramp_x))[0], upstream),
               (np.where(floor & (mid[:, 0] >= ramp_x))[0], WALL),
               (np.where((side == 1) | (side == 3))[0], OUTLET)]
     return _assemble(pts, tri, en, c0, c1, groups)
