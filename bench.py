@@ -522,21 +522,27 @@ def run_batch_scale(args, grp):
                                               kappa=mu * gamma * cv / 0.72, cv=cv)))
         q0.append(mg.freestream(mach, mesh.n_cells))
     setup_s = time.perf_counter() - t0
-    b = batch.Batch(cases, implicit=dict(max_iter=args.scale_iters, p_floor=P_FLOOR,
-                                         tol=1e-30),
-                    flux=1, order=2, limiter=1, precision=1, viscous=1)
-    b.set_state(q0)
-    grp.barrier()
-    r = b.solve()
     cells = int(sum(m.n_cells for m, _ in cases))
-    info = b.info()
-    b.close()
-    return {"cases": args.scale_cases, "cells": cells, "cell_range": list(args.scale_cells),
-            "iterations": r["iterations"], "device_s": round(r["ms"] * 1e-3, 3),
-            "Mcell_iterations_per_s": round(cells * r["iterations"] / (r["ms"] * 1e-3) / 1e6, 1),
-            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
-            "mesh_setup_s": round(setup_s, 1),
-            "precision": "FP64 residual and sweeps (the cold-start path)"}
+    out = {"cases": args.scale_cases, "cells": cells, "cell_range": list(args.scale_cells),
+           "mesh_setup_s": round(setup_s, 1)}
+    # the cold-start path (FP64 residual and sweeps) and the production
+    # options (FP32 residual -- the FP32 phase lasts the whole short run --
+    # and FP32 sweeps)
+    for label, imp in (("fp64", dict(p_floor=P_FLOOR)),
+                       ("production", dict(fp32_until=args.fp32_until, sweep_fp32=1,
+                                           p_floor=P_FLOOR))):
+        b = batch.Batch(cases, implicit=dict(imp, max_iter=args.scale_iters, tol=1e-30),
+                        flux=1, order=2, limiter=1, precision=1, viscous=1)
+        b.set_state(q0)
+        grp.barrier()
+        r = b.solve()
+        info = b.info()
+        b.close()
+        out[label] = {"iterations": r["iterations"], "device_s": round(r["ms"] * 1e-3, 3),
+                      "Mcell_iterations_per_s": round(cells * r["iterations"]
+                                                      / (r["ms"] * 1e-3) / 1e6, 1),
+                      "colors": info["n_colors"], "sweep_threads": info["sweep_threads"]}
+    return out
 
 
 def run_tgv3d(args, grp):
