@@ -373,8 +373,9 @@ typedef struct mst_implicit_params {
    * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
    * state) and switches to the FP64 residual once every unconverged case
    * is below fp32_until * L2_first or stagnating in FP32 (its L2 has not
-   * fallen by 10% for 500 iterations: the FP32 residual's floor); 0: FP64
-   * residual throughout */
+   * fallen by 10% for 500 iterations: the FP32 residual's floor), or once
+   * at least half are and no further case has joined them for 500
+   * iterations; 0: FP64 residual throughout */
   double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */

@@ -89,6 +89,7 @@ struct mst_batch {
   // phase-switch bookkeeping: per case the best FP32-phase L2 and when
   std::vector<double> lo_best;
   std::vector<int> lo_best_it;
+  int lo_ready_max = 0, lo_ready_since = 0;
   bool tuned = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [FP64 phase, FP32 phase]
   int graph_iters[2] = {0, 0};
@@ -511,6 +512,8 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   b->first_fixed = false;
   b->lo_best.clear();
   b->lo_best_it.clear();
+  b->lo_ready_max = 0;
+  b->lo_ready_since = 0;
   if (b->lo || b->sweep32) {
     cudaError_t e = mst::fast::launch_to_f32(b->ctx->q_old, b->ctx->qf_old, b->ctx->dm.n_cells,
                                              b->ctx->stream);
@@ -607,7 +610,7 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     done = h[1];
     if (done >= b->n_cases) break;
     if (b->lo) {
-      // leave the FP32 phase once every case is converged, below
+      // a case is ready to leave the FP32 phase once converged, below
       // fp32_until, or stagnating in FP32 (its L2 has not fallen by 10%
       // for 500 iterations: the FP32 residual's floor)
       B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
@@ -629,7 +632,15 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
         }
         if (iters - b->lo_best_it[i] >= 500) ++ready;
       }
-      if (ready == b->n_cases) {
+      if (ready > b->lo_ready_max) {
+        b->lo_ready_max = ready;
+        b->lo_ready_since = iters;
+      }
+      // all ready, or at least half ready and no further case for 500
+      // iterations (a case whose FP32 residual oscillates keeps setting
+      // new bests and would hold the whole batch in FP32)
+      if (ready == b->n_cases ||
+          (2 * b->lo_ready_max >= b->n_cases && iters - b->lo_ready_since >= 500)) {
         b->lo = false;
         st = ensure_graph();
         if (st) return st;
