@@ -382,8 +382,14 @@ def run_batch(args, ws, rank, grp):
     bm.close()
     if args.warm_train > 0:
         out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp)
-        if out["warm"].get("value"):
-            out["warm_speedup"] = round(out["value"] / out["warm"]["value"], 3)
+        w = out["warm"]
+        # a wall-time ratio only when the warm run reaches the tolerance on
+        # at least the cases the cold start did
+        if w.get("value") and w.get("converged", 0) >= out["converged"]:
+            out["warm_speedup"] = round(out["value"] / w["value"], 3)
+        else:
+            out["warm_speedup"] = None
+            out["warm_speedup_note"] = "the warm run converged fewer cases than the cold start"
     return out
 
 
