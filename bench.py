@@ -195,7 +195,8 @@ def _gemm_at_scale(net, feats):
             "tflops": round(tflops, 2), "tensor_frac": round(tflops / tf_peak, 4),
             "tensor_peak": tf_peak, "tensor_peak_source": tf_src,
             "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4), "hbm_peak_source": hbm_src,
-            "flops_per_byte": round(g["flops"] / g["bytes"], 1), "ridge_flops_per_byte": round(ridge, 1),
+            "flops_per_byte": round(g["flops"] / g["bytes"], 1),
+            "ridge_flops_per_byte": round(ridge, 1),
             "bound": "hbm" if g["flops"] / g["bytes"] < ridge else "tensor"}
 
 
@@ -310,6 +311,18 @@ def _wedge_cases(n_cases, lo, hi):
 P_FLOOR = 0.01
 
 
+def _production(args):
+    """Implicit parameters of the batch's production runs (warm start and
+    the matching cold start)."""
+    return dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1,
+                p_floor=P_FLOOR, fp32_window=args.fp32_window)
+
+
+def _production_label(args):
+    return (f"FP32 residual until L2 {args.fp32_until:g} (window {args.fp32_window}), then "
+            f"FP64; FP32 sweeps, FP64 diagonal inversion and update")
+
+
 def run_batch(args, ws, rank, grp):
     """Cold-start batched LU-SGS solve of the wedge family to L2 1e-8.  With
     N ranks the cases are split by greedy size balancing, each rank solves
@@ -366,7 +379,7 @@ def run_batch(args, ws, rank, grp):
     first_cold = st["first_l2"]
     b.close()
     # the same cold start with the FP32 residual until 1e-3 (then FP64)
-    bm = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
+    bm = batch.Batch(cases, implicit=_production(args),
                      flux=1, order=2, limiter=1, precision=1, viscous=1)
     bm.set_state(q0)
     grp.barrier()
@@ -378,7 +391,7 @@ def run_batch(args, ws, rank, grp):
     out["cold_mixed"] = {"value": round(grp.max(wall_m), 3), "unit": "s",
                          "converged": int(grp.sum((cm >= 0).sum())),
                          "iterations": rm["iterations"],
-                         "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update"}
+                         "precision": _production_label(args)}
     bm.close()
     if args.warm_train > 0:
         out["warm"] = run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp)
@@ -442,7 +455,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     q_warm = [ws.state(ws.predict(net, f, ptr, nbr), mach) for f, ptr, nbr, mach in feats]
     infer_s = time.perf_counter() - t2
     gemm = _gemm_at_scale(net, feats)
-    b = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1, p_floor=P_FLOOR),
+    b = batch.Batch(cases, implicit=_production(args),
                     flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q_warm)
     # the same residual tolerance as the cold start: L2 <= tol x the cold
@@ -467,7 +480,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     it_w = [int(conv[k]) for k in both]
     it_c = [int(conv_cold[k]) for k in both]
     return {"value": round(wall, 3), "unit": "s", "inference_s": round(infer_s, 3),
-            "precision": f"FP32 residual until L2 {args.fp32_until:g}, then FP64; FP32 sweeps, FP64 diagonal inversion and update",
+            "precision": _production_label(args),
             "tolerance": "L2 <= 1e-8 x the cold start's first-iteration L2 of each case "
                          "(the same absolute residual as the cold start)",
             "converged": int(grp.sum((conv >= 0).sum())), "iterations": r["iterations"],
@@ -536,6 +549,7 @@ def run_batch_scale(args, grp):
     # and FP32 sweeps)
     for label, imp in (("fp64", dict(p_floor=P_FLOOR)),
                        ("production", dict(fp32_until=args.fp32_until, sweep_fp32=1,
+                                           fp32_window=args.fp32_window,
                                            p_floor=P_FLOOR))):
         b = batch.Batch(cases, implicit=dict(imp, max_iter=args.scale_iters, tol=1e-30),
                         flux=1, order=2, limiter=1, precision=1, viscous=1)
@@ -661,6 +675,8 @@ def main():
     ap.add_argument("--warm-steps", type=int, default=400)
     ap.add_argument("--fp32-until", type=float, default=1e-5,
                     help="the batch's production runs use the FP32 residual until this L2")
+    ap.add_argument("--fp32-window", type=int, default=500,
+                    help="iterations of the FP32-phase stagnation / wait tests")
     ap.add_argument("--scale-cases", type=int, default=0,
                     help="cases of the batch-throughput line at scale (0: skip)")
     ap.add_argument("--scale-cells", type=int, nargs=2, default=[20000, 400000])

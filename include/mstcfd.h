@@ -373,9 +373,9 @@ typedef struct mst_implicit_params {
    * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
    * state) and switches to the FP64 residual once every unconverged case
    * is below fp32_until * L2_first or stagnating in FP32 (its L2 has not
-   * fallen by 10% for 500 iterations: the FP32 residual's floor), or once
-   * at least half are and no further case has joined them for 500
-   * iterations; 0: FP64 residual throughout */
+   * fallen by 10% for fp32_window iterations: the FP32 residual's floor),
+   * or once at least half are and no further case has joined them for
+   * fp32_window iterations; 0: FP64 residual throughout */
   double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
@@ -391,7 +391,10 @@ typedef struct mst_implicit_params {
    * momentum kept).  Without it a near-vacuum cell at a slip / no-slip
    * corner rejects every update (positivity) and freezes its case. */
   double p_floor;
-  int reserved[2];
+  /* iterations of the FP32-phase tests (stagnation window, wait for
+   * further cases); 0 = 500 */
+  int fp32_window;
+  int reserved[1];
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,

@@ -612,7 +612,7 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     if (b->lo) {
       // a case is ready to leave the FP32 phase once converged, below
       // fp32_until, or stagnating in FP32 (its L2 has not fallen by 10%
-      // for 500 iterations: the FP32 residual's floor)
+      // for win iterations: the FP32 residual's floor)
       B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
@@ -620,6 +620,7 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
         b->lo_best.assign(b->n_cases, 1e300);
         b->lo_best_it.assign(b->n_cases, iters);
       }
+      const int win = b->ip.fp32_window > 0 ? b->ip.fp32_window : 500;
       int ready = 0;
       for (int i = 0; i < b->n_cases; ++i) {
         if (cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i]) {
@@ -630,17 +631,17 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
           b->lo_best[i] = l[i];
           b->lo_best_it[i] = iters;
         }
-        if (iters - b->lo_best_it[i] >= 500) ++ready;
+        if (iters - b->lo_best_it[i] >= win) ++ready;
       }
       if (ready > b->lo_ready_max) {
         b->lo_ready_max = ready;
         b->lo_ready_since = iters;
       }
-      // all ready, or at least half ready and no further case for 500
+      // all ready, or at least half ready and no further case for win
       // iterations (a case whose FP32 residual oscillates keeps setting
       // new bests and would hold the whole batch in FP32)
       if (ready == b->n_cases ||
-          (2 * b->lo_ready_max >= b->n_cases && iters - b->lo_ready_since >= 500)) {
+          (2 * b->lo_ready_max >= b->n_cases && iters - b->lo_ready_since >= win)) {
         b->lo = false;
         st = ensure_graph();
         if (st) return st;
