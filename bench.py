@@ -675,7 +675,7 @@ def main():
     ap.add_argument("--warm-steps", type=int, default=400)
     ap.add_argument("--fp32-until", type=float, default=1e-5,
                     help="the batch's production runs use the FP32 residual until this L2")
-    ap.add_argument("--fp32-window", type=int, default=500,
+    ap.add_argument("--fp32-window", type=int, default=1000,
                     help="iterations of the FP32-phase stagnation / wait tests")
     ap.add_argument("--scale-cases", type=int, default=0,
                     help="cases of the batch-throughput line at scale (0: skip)")
