@@ -472,6 +472,27 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
     qw = b.state()
     b.close()
     net.close()
+    # the network's own effect: the same warm start on the plain FP64 path
+    # (the cold start's settings), against the cold start
+    bf = batch.Batch(cases, implicit=dict(max_iter=args.batch_iters, p_floor=P_FLOOR),
+                     flux=1, order=2, limiter=1, precision=1, viscous=1)
+    bf.set_state(q_warm)
+    bf.set_l2_ref(first_cold)
+    grp.barrier()
+    t4 = time.perf_counter()
+    bf.solve()
+    wall_f = grp.max(infer_s + time.perf_counter() - t4)
+    conv_f = bf.case_status()["conv_iter"]
+    bf.close()
+    both_f = [k for k in range(len(cases)) if conv_f[k] >= 0 and conv_cold[k] >= 0]
+    warm_fp64 = {"value": round(wall_f, 3), "unit": "s",
+                 "converged": int(grp.sum((conv_f >= 0).sum())),
+                 "precision": "FP64 residual and sweeps (the cold start's settings)",
+                 "iteration_ratio_cold_over_warm": round(
+                     float(np.sum([conv_cold[k] for k in both_f]))
+                     / max(float(np.sum([conv_f[k] for k in both_f])), 1.0), 3)
+                 if both_f else None,
+                 "case_iterations": [int(x) for x in conv_f]}
     both = [k for k in range(len(cases)) if conv[k] >= 0 and conv_cold[k] >= 0]
     diff = max((float(np.abs(qw[k] - q_cold[k]).max() / np.abs(q_cold[k]).max()) for k in both),
                default=None)
@@ -499,7 +520,7 @@ def run_warm(args, fam, cases, q_cold, conv_cold, first_cold, grp):
                       "loss_first": round(float(hist[0]), 5),
                       "loss_last": round(float(hist[-20:].mean()), 5),
                       "data_s": round(data_s, 2), "train_s": round(train_s, 2)},
-            "network_gemm": gemm}
+            "network_gemm": gemm, "warm_fp64": warm_fp64}
 
 
 def run_cpu_sample(m, steps, budget_s=30.0):
