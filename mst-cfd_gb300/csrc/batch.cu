@@ -81,6 +81,7 @@ struct mst_batch {
   float4* dqf = nullptr;         // FP32 sweeps: dQ* / dQ in FP32
   bool sweep32 = false;
   bool first_fixed = false;      // reference L2s set by mst_batch_set_l2_ref
+  double* norm_part = nullptr;   // [n_cases][8] partial L2 sums
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
   // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
   // lo is set, FP64 afterwards; the sweeps are FP64 throughout
@@ -232,6 +233,7 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.l2_win = b->l2_win;
   na.freeze_tol = b->ip.freeze_tol;
   na.first_fixed = b->first_fixed ? 1 : 0;
+  na.part = b->norm_part;
   na.cfl0 = b->ip.cfl0;
   na.cfl_max = b->ip.cfl_max;
   na.tol = b->ip.tol;
@@ -448,6 +450,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->dq, sizeof(double4_32a) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->diag, sizeof(double) * (size_t)nC)) ||
       (st = balloc(b.get(), &b->dqf, b->sweep32 ? sizeof(float4) * (size_t)nC : 0)) ||
+      (st = balloc(b.get(), &b->norm_part, sizeof(double) * 8 * (size_t)n_cases)) ||
       (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
                                             ? sizeof(float) * 8 * (size_t)nC : 0)) ||
       (st = reset_progress(b.get()))) {

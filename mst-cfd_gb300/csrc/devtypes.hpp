@@ -174,6 +174,7 @@ struct CaseNormArgs {
   double* l2_win;          // [n_cases] L2 at the last freezing-window check
   double cfl0, cfl_max, tol, freeze_tol;
   int first_fixed;         // first[] holds reference L2s set by the caller
+  double* part;            // [n_cases][8] partial sums of (R_rho / V)^2
 };
 
 // Precisions / schemes (mirrors of the public enums)
