@@ -16,6 +16,7 @@ REF_OUT = os.path.join(HERE, "_ref")
 REF_SRC = os.environ.get("MSTCFD_REF_SRC", "/root/reference/MST-CFD")
 
 _SOURCES = ["mstoracle.c", "mstoracle_ext.c", "mstoracle_lu.c", "mstoracle_io.c",
+            "mstoracle_simple.c",
             "mstoracle_implicit.c", "mstoracle3d.c"]
 
 
@@ -47,10 +48,10 @@ def build_ref(force=False):
     sources are not present on this machine."""
     if not ref_available():
         return False
-    marker = os.path.join(REF_OUT, "ref_mesh3d")
+    marker = os.path.join(REF_OUT, "ref_simple_mt")
     deps = [os.path.join(HERE, "ref", f) for f in
             ("build_ref.sh", "harness_rho.cpp", "harness_lu.cpp", "harness_io.cpp",
-             "harness_mesh3d.cpp",
+             "harness_mesh3d.cpp", "harness_simple.cpp",
              os.path.join("eigen_shim", "Eigen", "shim_matrix.h"))]
     if force or _stale(marker, deps):
         env = dict(os.environ, MSTCFD_REF_SRC=REF_SRC, MSTCFD_REF_OUT=REF_OUT)

@@ -177,6 +177,25 @@ int om_step_ext(const om_mesh *m, const om_params_ext *p, double *q,
 /* Scalar SparseSolverNUM::solveILUSGS (gs = 0) or solveGS (gs = 1) on the
  * system built by the ordered insertions (rows[i], cols[i], vals[i]) with
  * ops[i] = 0 setELE, 1 addELE.  x: initial guess in, solution out. */
+/* ---- pressure-based SIMPLE (mstoracle_simple.c) ---- */
+typedef struct om_simple_params {
+  double dt;          /* 1 / STEP_TIME */
+  double alpha_p;     /* SIMPLE_ALPHA_P: p += alpha_p p' */
+  int n_inner;        /* SIMPLE_INTERVAL: SIMPLE iterations per step */
+  int wall_smooth;    /* FLAG_WALLSMOOTH */
+  double inlet[4];    /* face (p, u, v, T) on inlet (type 10) faces */
+  double p_out;       /* face pressure on outlet (type 5) faces */
+} om_simple_params;
+void om_simple_default_params(om_simple_params *p);
+/* (p, u, v, T) of conserved states, as Time::initialization forms them */
+void om_q_to_puvt(int n, const double *q, double *puvt);
+/* nsteps time steps; puvt [n_cells][4] and face [n_faces][4] in/out;
+ * time_rows [nsteps][4], inner_rows [nsteps][n_inner][4] and gs_iters
+ * [nsteps][n_inner][3] (u, v, p' solves) may be NULL */
+int om_simple_step(const om_mesh *m, const om_simple_params *p, double *puvt,
+                   double *face, int nsteps, double *time_rows, double *inner_rows,
+                   int *gs_iters);
+
 int om_lu_scalar(int gs, int dim, int n, const int *rows, const int *cols,
                  const int *ops, const double *vals, const double *b, double *x,
                  int *iterations);

@@ -60,6 +60,12 @@ class _ONorms(C.Structure):
 _lib = None
 
 
+class _OSimple(C.Structure):
+    _fields_ = [("dt", C.c_double), ("alpha_p", C.c_double), ("n_inner", C.c_int),
+                ("wall_smooth", C.c_int), ("inlet", C.c_double * 4),
+                ("p_out", C.c_double)]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -102,6 +108,10 @@ def lib():
         L.om_lusgs_iterate.argtypes = [C.POINTER(_OMesh), C.POINTER(_OParamsExt), _dp, _ip,
                                        C.POINTER(_OLusgs), C.c_int, _dp]
         L.om_greedy_colors.argtypes = [C.POINTER(_OMesh), _ip]
+        L.om_simple_default_params.argtypes = [C.POINTER(_OSimple)]
+        L.om_q_to_puvt.argtypes = [C.c_int, _dp, _dp]
+        L.om_simple_step.argtypes = [C.POINTER(_OMesh), C.POINTER(_OSimple), _dp, _dp,
+                                     C.c_int, _dp, _dp, _ip]
         _lib = L
     return _lib
 
@@ -554,3 +564,39 @@ def kinetic_energy3(mesh, q):
     ke, v = C.c_double(), C.c_double()
     lib3().om3_kinetic_energy(C.byref(mesh._m), _d(_f64(q)), C.byref(ke), C.byref(v))
     return ke.value, v.value
+
+
+# ---- pressure-based SIMPLE (mstoracle_simple.c) ----
+def simple_params(**kw):
+    p = _OSimple()
+    lib().om_simple_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "inlet":
+            for i in range(4):
+                p.inlet[i] = v[i]
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def q_to_puvt(q):
+    q = _f64(q).reshape(-1, 4)
+    out = np.zeros_like(q)
+    lib().om_q_to_puvt(len(q), _d(q), _d(out))
+    return out
+
+
+def simple_step(mesh, puvt, face, nsteps=1, prm=None):
+    """nsteps SIMPLE time steps; returns (puvt, face, time rows, SIMPLE
+    iteration rows, Gauss-Seidel iteration counts)."""
+    prm = prm or simple_params()
+    pv = _f64(puvt).reshape(-1, 4).copy()
+    fc = _f64(face).reshape(-1, 4).copy()
+    rows = np.zeros((nsteps, 4))
+    inner = np.zeros((nsteps, prm.n_inner, 4))
+    its = np.zeros((nsteps, prm.n_inner, 3), np.int32)
+    rc = lib().om_simple_step(mesh._p, C.byref(prm), _d(pv), _d(fc), int(nsteps),
+                              _d(rows), _d(inner), _i(its))
+    if rc != 0:
+        raise RuntimeError(f"om_simple_step failed ({rc})")
+    return pv, fc, rows, inner, its

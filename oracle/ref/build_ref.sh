@@ -116,9 +116,39 @@ $CXX $CXXFLAGS -I"$S3" -c "$HERE/harness_mesh3d.cpp" -o "$O3/harness_mesh3d.o" &
 wait
 $CXX $CXXFLAGS $objs3 "$O3/harness_mesh3d.o" -o "$OUT/ref_mesh3d"
 
+# Pressure-based SIMPLE path (harness_simple.cpp): the density-based sources
+# plus pSolver/SolverSIMPLE.cpp, whose header only needs the (empty)
+# PSolver.h overlay.  "simple" runs one thread: the reference's SIMPLE
+# residual maximum is a data race across OpenMP threads
+# (SolverSIMPLE.cpp:62-71); "simple_mt" uses every host thread and is the
+# timed CPU baseline.
+build_simple() {  # variant-dir threads
+  local V=$1 T=$2
+  mirror "$V" 1 SolverAusm
+  local S="$OUT/$V/src" O="$OUT/$V/obj"
+  printf '#undef NUM_CPU_THREADS\n#define NUM_CPU_THREADS %s\n' "$T" >> "$S/include/CONST.h"
+  ln -s "$REF/pSolver/SolverSIMPLE.h" "$S/pSolver/SolverSIMPLE.h"
+  ln -s "$REF/pSolver/SolverSIMPLE.cpp" "$S/pSolver/SolverSIMPLE.cpp"
+  mkdir -p "$O"
+  local objs=""
+  for f in $SRCS lusolver/SparseSolverNUM.cpp pSolver/SolverSIMPLE.cpp; do
+    local o="$O/$(echo "$f" | tr '/' '_').o"
+    objs="$objs $o"
+    $CXX $CXXFLAGS -I"$S" -c "$S/$f" -o "$o" &
+  done
+  $CXX $CXXFLAGS -I"$S" -c "$HERE/harness_simple.cpp" -o "$O/harness_simple.o" &
+  wait
+  $CXX $CXXFLAGS $objs "$O/harness_simple.o" -o "$OUT/ref_$V"
+}
+build_simple simple 1 &
+build_simple simple_mt "$THREADS" &
+wait
+
 for v in ausm_o1 ausm_o2 roe_o1 roe_o2; do
   test -x "$OUT/ref_rho_$v"
 done
+test -x "$OUT/ref_simple"
+test -x "$OUT/ref_simple_mt"
 test -x "$OUT/ref_mesh3d"
 test -x "$OUT/ref_lu"
 test -x "$OUT/ref_io"

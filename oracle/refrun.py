@@ -135,6 +135,47 @@ def run_io(mesh_path, q, zone_t=0, time_now=0):
     return plt, cell, back
 
 
+def run_simple(mesh_path, puvt0=None, steps=1, threads=1, bench=0):
+    """The reference's SIMPLE solver (oracle/ref/harness_simple.cpp): dict
+    with the cell and face (p, u, v, T) after ``steps`` time steps, the Time
+    rows, the SIMPLE iteration rows and the Gauss-Seidel iteration counts
+    (u, v, p' per SIMPLE iteration).  ``bench`` > 0: seconds per step."""
+    if not _build.build_ref():
+        raise RuntimeError("reference sources not available")
+    exe = os.path.join(_build.REF_OUT, "ref_simple" if threads == 1 else "ref_simple_mt")
+    d = tempfile.mkdtemp(prefix="mstsimple_")
+    args = [exe, os.path.abspath(mesh_path), d]
+    if puvt0 is not None:
+        pp = os.path.join(d, "puvt0_in.f64")
+        np.ascontiguousarray(puvt0, dtype=np.float64).tofile(pp)
+        args += ["--puvt0", pp]
+    if bench:
+        r = subprocess.run(args + ["--bench", str(int(bench))], check=True,
+                           capture_output=True, text=True)
+        return float(r.stdout.strip().splitlines()[-1])
+    subprocess.run(args + ["--steps", str(int(steps))], check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    out = dict(
+        puvt=np.fromfile(os.path.join(d, "puvt.f64")).reshape(-1, 4),
+        face=np.fromfile(os.path.join(d, "face_sc.f64")).reshape(-1, 4),
+        time_rows=np.fromfile(os.path.join(d, "time_rows.f64")).reshape(-1, 4))
+    with open(os.path.join(d, "time.log")) as f:
+        out["inner_rows"] = np.array([[float(x) for x in ln.split()] for ln in f
+                                      if ln.strip()])
+    its, n = [], 0
+    with open(os.path.join(d, "gs.log")) as f:
+        for ln in f:
+            if ln.startswith("LU-residual-GS"):
+                k = int(ln.split()[1])
+                if k == 0 and n:
+                    its.append(n)
+                n = k + 1
+    if n:
+        its.append(n)
+    out["gs_iters"] = np.array(its, np.int32).reshape(-1, 3)
+    return out
+
+
 def run_mesh3d(mesh_path):
     """The reference's 3D reader (oracle/ref/harness_mesh3d.cpp): dict of
     its arrays."""
