@@ -677,6 +677,58 @@ def run_tgv3d(args, grp):
     return out
 
 
+def run_simple(args, grp):
+    """Pressure-based SIMPLE time steps (the reference's default solver:
+    PSolver with SolverSIMPLE, 5 SIMPLE iterations per step, DT = 1/4000)
+    on triangle channels with inlet, outlet and wall zones from the
+    reference's initial field: time steps per second of mst_simple_step
+    (one kernel launch per call, wall clock around the call), and the
+    oracle's single-thread CPU time on the same meshes."""
+    import tempfile
+    from mstcfd import Mesh
+    from mstcfd import meshgen as mg
+    from mstcfd.psolver import SimpleSolver, reference_initial
+    out = {"workload": "SIMPLE (SolverSIMPLE) on jittered triangle channels 2 x 1, inlet / "
+                       "outlet / walls, the reference's split initial field, DT = 1/4000, "
+                       "5 SIMPLE iterations per step, FP64 bit-exact",
+           "unit": "time steps/s"}
+    d = tempfile.mkdtemp(prefix="bench_simple_")
+    for label, nx, ny, steps in (("sod_size", 95, 96, 40), ("large", 400, 300, 10)):
+        path = os.path.join(d, label + ".msh")
+        mg.write_msh(path, mg.reorient(mg.tri_box(nx, ny, 2.0, 1.0, jitter=0.2, seed=5,
+                                                  left=mg.INLET, right=mg.OUTLET,
+                                                  bottom=mg.WALL, top=mg.WALL),
+                                       "random", seed=6))
+        mesh = Mesh.read_msh(path)
+        s = SimpleSolver(mesh)
+        s.step(max(3, args.warmup))
+        grp.barrier()
+        t0 = time.perf_counter()
+        s.step(steps)
+        secs = grp.max(time.perf_counter() - t0)
+        i = s.info()
+        res = {"cells": mesh.n_cells, "faces": mesh.n_faces, "steps": steps,
+               "value": round(steps * grp.ws / secs, 2), "ms_per_step": round(1e3 * secs / steps, 3),
+               "gpu_launches": 1, "cluster_ctas": i.cluster, "threads_per_cta": i.threads,
+               "gauss_seidel_levels": [i.momentum_levels, i.pressure_levels]}
+        s.close()
+        if not args.no_cpu and grp.ws == 1:
+            from oracle import build as ob
+            from oracle import pyoracle as po
+            ob.build_oracle()
+            om = po.read_msh(path)
+            p0, f0 = reference_initial(mesh)
+            n_cpu = 2 if mesh.n_cells < 100000 else 1
+            t1 = time.perf_counter()
+            po.simple_step(om, p0, f0, n_cpu)
+            cs = time.perf_counter() - t1
+            res["cpu_baseline"] = {"value": round(n_cpu / cs, 3), "unit": "time steps/s",
+                                   "cores": 1, "kind": "port",
+                                   "sample": f"{n_cpu} step(s) of the same mesh ({cs:.2f} s)"}
+        out[label] = res
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -705,6 +757,8 @@ def main():
     ap.add_argument("--tgv-n", type=int, default=128,
                     help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
     ap.add_argument("--tgv-steps", type=int, default=10)
+    ap.add_argument("--no-simple", action="store_true",
+                    help="skip the pressure-based SIMPLE sub-line")
     args = ap.parse_args()
     ws, rank, local = _dist()
     workload = (f"isentropic vortex, periodic jittered Delaunay {args.n}x{args.n} "
@@ -742,6 +796,7 @@ def main():
     batch_line = run_batch(args, ws, rank, grp) if args.batch_cases > 0 else None
     tgv_line = run_tgv3d(args, grp) if args.tgv_n > 0 else None
     scale_line = run_batch_scale(args, grp) if args.scale_cases > 0 else None
+    simple_line = None if args.no_simple else run_simple(args, grp)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         m = _workload(args.n)
@@ -763,7 +818,7 @@ def main():
                     for k, v in results["e2e"].items()},
             "gpu_launches": fp32["launches"],
             "roofline": roof, "cpu_baseline": cpu, "clocks": results.get("clocks"),
-            "batch": batch_line, "tgv3d": tgv_line}
+            "batch": batch_line, "tgv3d": tgv_line, "simple": simple_line}
     if scale_line:
         line["batch_scale"] = scale_line
     print(json.dumps(line))

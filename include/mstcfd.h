@@ -579,6 +579,68 @@ mst_status mst_lu_solve(mst_lu *s, int method, const double *b, double *x,
 mst_status mst_lu_levels(const mst_lu *s, int *forward, int *backward);
 mst_status mst_lu_destroy(mst_lu *s);
 
+/* ------------------------------------------------------------------ */
+/* pressure-based SIMPLE solver (the reference's PSolver/SolverSIMPLE) */
+/* ------------------------------------------------------------------ */
+/* Replaces PSolver (pSolver/PSolver.h:16-41) with PSOLVER = SolverSIMPLE
+ * (pSolver/SolverSIMPLE.h:20-80), the solver the reference's CONST.h
+ * selects (RHO_P 1).  States are (p, u, v, T) per cell ([n_cells][4], file
+ * cell order, as AllData's pNewCellPUVT) and per face ([n_faces][4], as
+ * pFacePUVTSC).  Results are bit-identical to the reference's SolverSIMPLE
+ * (one OpenMP thread; the reference's residual maximum races across
+ * threads, its state does not). */
+typedef struct mst_simple mst_simple;
+typedef struct mst_simple_params {
+  double dt;          /* PSolver::setDT (reference: 1 / STEP_TIME) */
+  double alpha_p;     /* SIMPLE_ALPHA_P: p += alpha_p p' */
+  int n_inner;        /* SIMPLE_INTERVAL: SIMPLE iterations per step */
+  int wall_smooth;    /* FLAG_WALLSMOOTH: 1 reflects the wall velocity,
+                         0 sets it to zero (SolverSIMPLE.cpp:131-138) */
+  double inlet[4];    /* face (p, u, v, T) of inlet (type 10) faces */
+  double p_out;       /* face pressure of outlet (type 5) faces */
+  int cluster;        /* CTAs of the kernel's thread-block cluster, 0 = the
+                         largest that fits (16, 8, 4, 2 or 1) */
+  int reserved[3];
+} mst_simple_params;
+typedef struct mst_simple_info {
+  int n_cells, n_faces;
+  int cluster, threads;               /* launch shape of the step kernel */
+  int momentum_levels, pressure_levels; /* Gauss-Seidel sweep levels */
+  int last_steps;                     /* steps of the last mst_simple_step */
+  int reserved;
+} mst_simple_info;
+
+/* The reference's CONST.h values: dt = 1/4000, alpha_p = 0.3, n_inner = 5,
+ * wall_smooth = 1, inlet = (getP(inletQ), 0, 0, inletT) and p_out =
+ * getP(iniQ) (SolverSIMPLE.cpp:110-112, :168-175). */
+mst_status mst_simple_default_params(mst_simple_params *p);
+/* (p, u, v, T) of conserved states (rho, rho u, rho v, E) as
+ * Time::initialization forms them (time/Time.cpp:21-23; getP/getT,
+ * work/FUNCTION.cpp:7-14).  Host only. */
+mst_status mst_q_to_puvt(int n, const double *q, double *puvt);
+/* params may be NULL (defaults).  Periodic meshes: MST_EUNSUPPORTED. */
+mst_status mst_simple_create(const mst_mesh *m, const mst_simple_params *p,
+                             mst_simple **out);
+/* Host arrays.  The old time level is set to the same state
+ * (Time::initialization).  face_puvt may be NULL: face values are kept
+ * (zero after create); faces of zone types the reference's face update
+ * skips (e.g. 7) keep their values for the whole run. */
+mst_status mst_simple_set_state(mst_simple *s, const double *cell_puvt,
+                                const double *face_puvt);
+mst_status mst_simple_get_state(mst_simple *s, double *cell_puvt, double *face_puvt);
+/* nsteps time steps, each Time::goNextTimeStep with RHO_P 1 (time/Time.cpp:
+ * 54-80): a SolverSIMPLE solve of n_inner iterations, then new -> old.
+ * time_rows (nullable) receives [nsteps][4] max |new - old| / old per
+ * component (the Time loop's log row).  One kernel launch. */
+mst_status mst_simple_step(mst_simple *s, int nsteps, double *time_rows);
+/* Of the last mst_simple_step: the SIMPLE iteration rows
+ * [nsteps][n_inner][4] (max |new - old| / (old + EOR), SolverSIMPLE.cpp:
+ * 62-71) and the Gauss-Seidel iterations of the u, v and p' solves
+ * [nsteps][n_inner][3] (each at most LU_INTERVAL).  Either may be NULL. */
+mst_status mst_simple_rows(mst_simple *s, double *inner_rows, int *gs_iters);
+mst_status mst_simple_get_info(const mst_simple *s, mst_simple_info *info);
+mst_status mst_simple_destroy(mst_simple *s);
+
 /* Per-kernel CUDA-event timing on the context's stream.  When enabled,
  * every kernel launch of mst_solve/mst_step is bracketed by events; the
  * totals accumulate until mst_profile_reset. */

@@ -8,6 +8,7 @@ Translation units are compiled in parallel for sm_103a only:
   * csrc/capi.cu           the C ABI of include/mstcfd.h
   * csrc/noalloc.cu        the allocation-free solve entry point
   * csrc/lusgs.cu          level-scheduled LU-SGS / GS sweeps, --fmad=false
+  * csrc/simple.cu         the pressure-based SIMPLE solver, --fmad=false
   * csrc/io.cu             result writer (device node averaging) and
                            checkpoint files, --fmad=false
   * csrc/batch.cu          batched steady solves (LU-SGS orchestration,
@@ -59,6 +60,7 @@ def _units():
         ("capi.o", [nv] + common + ["-c", os.path.join(CSRC, "capi.cu")]),
         ("noalloc.o", [nv] + common + ["-c", os.path.join(CSRC, "noalloc.cu")]),
         ("lusgs.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "lusgs.cu")]),
+        ("simple.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "simple.cu")]),
         ("io.o", [nv] + common + ["--fmad=false", "-c", os.path.join(CSRC, "io.cu")]),
         ("batch.o", [nv] + common + ["-c", os.path.join(CSRC, "batch.cu")]),
         ("mpnn.o", [nv] + common + ["-c", os.path.join(CSRC, "mpnn.cu")]),

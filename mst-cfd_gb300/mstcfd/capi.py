@@ -114,6 +114,18 @@ class Norms(C.Structure):
                 ("dt", C.c_double), ("time", C.c_double), ("mass", C.c_double)]
 
 
+class SimpleParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("alpha_p", C.c_double), ("n_inner", C.c_int),
+                ("wall_smooth", C.c_int), ("inlet", C.c_double * 4), ("p_out", C.c_double),
+                ("cluster", C.c_int), ("reserved", C.c_int * 3)]
+
+
+class SimpleInfo(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("cluster", C.c_int),
+                ("threads", C.c_int), ("momentum_levels", C.c_int),
+                ("pressure_levels", C.c_int), ("last_steps", C.c_int), ("reserved", C.c_int)]
+
+
 class MstError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"mstcfd status {status}: {msg}")
@@ -234,6 +246,16 @@ def load():
         "mst_lu_solve": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip]),
         "mst_lu_levels": (C.c_int, [C.c_void_p, _ip, _ip]),
         "mst_lu_destroy": (C.c_int, [C.c_void_p]),
+        "mst_simple_default_params": (C.c_int, [C.POINTER(SimpleParams)]),
+        "mst_q_to_puvt": (C.c_int, [C.c_int, _dp, _dp]),
+        "mst_simple_create": (C.c_int, [C.c_void_p, C.POINTER(SimpleParams),
+                                        C.POINTER(C.c_void_p)]),
+        "mst_simple_set_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "mst_simple_get_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "mst_simple_step": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "mst_simple_rows": (C.c_int, [C.c_void_p, _dp, _ip]),
+        "mst_simple_get_info": (C.c_int, [C.c_void_p, C.POINTER(SimpleInfo)]),
+        "mst_simple_destroy": (C.c_int, [C.c_void_p]),
         "mst_last_error": (C.c_char_p, []),
         "mst_abi_version": (C.c_int, []),
     }

@@ -56,7 +56,7 @@ def golden_cases():
     out = []
     if os.path.isdir(GOLDEN):
         for f in sorted(os.listdir(GOLDEN)):
-            if f.endswith(".npz") and not f.startswith(("lusolver", "writer")):
+            if f.endswith(".npz") and not f.startswith(("lusolver", "writer", "simple")):
                 out.append(os.path.join(GOLDEN, f))
     return out
 

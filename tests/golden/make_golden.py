@@ -17,7 +17,13 @@ text checkpoint the reference's own Work members write for them
 (oracle/ref/harness_io.cpp), and lusolver.npz: sparse systems with a mesh's sparsity, inserted in a
 shuffled order (setELE/addELE mixed, duplicates kept), solved by the
 reference's SparseSolverNUM::solveILUSGS / solveGS and
-SparseSolver<Matrix4d, Vector4d>::solveILU (oracle/ref/harness_lu.cpp).
+SparseSolver<Matrix4d, Vector4d>::solveILU (oracle/ref/harness_lu.cpp),
+and simple.npz: generated meshes with inlet, outlet, wall and symmetry
+zones run through the reference's pressure-based SolverSIMPLE
+(oracle/ref/harness_simple.cpp: Time::initialization, then per step a
+SolverSIMPLE solve with DT = 1/4000), from its own initial field and from
+a random (p, u, v, T) state: the initial and final cell and face values,
+the Time loop's residual rows and the Gauss-Seidel iteration counts.
 The GPU tests compare the CUDA path against these arrays bit-for-bit on
 machines where the reference is absent.
 
@@ -155,6 +161,45 @@ def make_io():
     return path
 
 
+def simple_cases():
+    yield "tri_iow", mg.reorient(mg.tri_box(16, 9, 1.0, 0.6, jitter=0.2, seed=3, left=mg.INLET,
+                                           right=mg.OUTLET, bottom=mg.WALL, top=mg.WALL),
+                                "random", seed=4), 3
+    yield "tri_sym", mg.reorient(
+        mg.tri_box(12, 8, 1.0, 0.6, jitter=0.25, seed=9, left=mg.WALL, right=mg.OUTLET,
+                   bottom=mg.SYMMETRY, top=mg.INLET), "fluent"), 3
+
+
+def random_puvt(n, seed):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.uniform(0.5, 1.5, n), rng.uniform(-0.3, 0.3, n),
+                     rng.uniform(-0.3, 0.3, n), rng.uniform(0.8, 1.2, n) / 286.32], 1)
+
+
+def make_simple():
+    out = {}
+    for name, mesh, steps in simple_cases():
+        d = tempfile.mkdtemp(prefix="golden_simple_")
+        msh = os.path.join(d, name + ".msh")
+        mg.write_msh(msh, mesh, crlf=True)
+        out[name + "_msh"] = np.frombuffer(open(msh, "rb").read(), np.uint8)
+        out[name + "_steps"] = np.array(steps)
+        init = refrun.run_simple(msh, steps=0)
+        r = refrun.run_simple(msh, steps=steps)
+        out[name + "_init_puvt"] = init["puvt"]
+        out[name + "_init_face"] = init["face"]
+        for k in ("puvt", "face", "time_rows", "gs_iters"):
+            out[f"{name}_init_{k}_out"] = r[k]
+        p0 = random_puvt(int(mesh["n_cells"]), seed=41)
+        r = refrun.run_simple(msh, puvt0=p0, steps=2)
+        out[name + "_rand_puvt"] = p0
+        for k in ("puvt", "face", "time_rows", "gs_iters"):
+            out[f"{name}_rand_{k}_out"] = r[k]
+    path = os.path.join(OUT, "simple.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 if __name__ == "__main__":
     for name, mesh in cases():
         p = make(name, mesh)
@@ -162,4 +207,6 @@ if __name__ == "__main__":
     p = make_lu()
     print(p, os.path.getsize(p))
     p = make_io()
+    print(p, os.path.getsize(p))
+    p = make_simple()
     print(p, os.path.getsize(p))
