@@ -726,6 +726,28 @@ def run_simple(args, grp):
                                    "cores": 1, "kind": "port",
                                    "sample": f"{n_cpu} step(s) of the same mesh ({cs:.2f} s)"}
         out[label] = res
+    # several independent cases in one launch, one thread-block cluster each
+    from mstcfd.psolver import step_batch
+    n_cases, steps = 8, 20
+    solvers = []
+    for k in range(n_cases):
+        path = os.path.join(d, f"case{k}.msh")
+        mg.write_msh(path, mg.reorient(mg.tri_box(95, 96, 2.0, 1.0, jitter=0.2, seed=30 + k,
+                                                  left=mg.INLET, right=mg.OUTLET,
+                                                  bottom=mg.WALL, top=mg.WALL),
+                                       "random", seed=60 + k))
+        solvers.append(SimpleSolver(Mesh.read_msh(path)))
+    step_batch(solvers, 2)
+    grp.barrier()
+    t0 = time.perf_counter()
+    step_batch(solvers, steps)
+    secs = grp.max(time.perf_counter() - t0)
+    out["batch"] = {"cases": n_cases, "cells_per_case": solvers[0].n_cells, "steps": steps,
+                    "value": round(n_cases * steps * grp.ws / secs, 2),
+                    "unit": "case time steps/s", "ms_per_batch_step": round(1e3 * secs / steps, 3),
+                    "gpu_launches": 1, "note": "mst_simple_step_batch: one cluster per case"}
+    for s_ in solvers:
+        s_.close()
     return out
 
 

@@ -633,6 +633,12 @@ mst_status mst_simple_get_state(mst_simple *s, double *cell_puvt, double *face_p
  * time_rows (nullable) receives [nsteps][4] max |new - old| / old per
  * component (the Time loop's log row).  One kernel launch. */
 mst_status mst_simple_step(mst_simple *s, int nsteps, double *time_rows);
+/* nsteps time steps of n independent cases (same cluster size) in ONE
+ * launch, one thread-block cluster per case, so that several cases fill
+ * the GPU; each case's results are those of mst_simple_step.  time_rows
+ * (nullable): [n][nsteps][4]. */
+mst_status mst_simple_step_batch(mst_simple *const *cases, int n, int nsteps,
+                                 double *time_rows);
 /* Of the last mst_simple_step: the SIMPLE iteration rows
  * [nsteps][n_inner][4] (max |new - old| / (old + EOR), SolverSIMPLE.cpp:
  * 62-71) and the Gauss-Seidel iterations of the u, v and p' solves

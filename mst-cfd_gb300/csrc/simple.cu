@@ -90,7 +90,7 @@ struct SimpleDev {
   double* rho_f;          // [nF] density of the face values (face pass)
   double* rho_o;          // [nC] density of the old time level
   const double *cf_dist, *cf_dn;  // [tot] |x_c - x_nb| and |S| per cell-face
-  double* part;           // [gridDim][kPart]
+  double* part;           // [cluster CTAs][kPart]
   double* time_rows;      // [steps][4]
   double* inner_rows;     // [steps][n_inner][4]
   int* gs_iters;          // [steps][n_inner][3]
@@ -124,7 +124,8 @@ __device__ __forceinline__ double dmax(double m, double q) { return (m < q) ? q 
 
 __device__ __forceinline__ void cluster_sync() { cg::this_cluster().sync(); }
 
-// CTA maximum of K values into part[blockIdx.x][0..K); callers cluster_sync()
+// CTA maximum of K values into part[CTA rank in the cluster][0..K); callers
+// cluster_sync()
 // before reading the partials
 template <int K>
 __device__ void cta_max(double (&v)[K], double* part) {
@@ -138,12 +139,13 @@ __device__ void cta_max(double (&v)[K], double* part) {
     for (int k = 0; k < K; ++k) {
       double m = red[0][k];
       for (int w = 1; w < kThreads / 32; ++w) m = dmax(m, red[w][k]);
-      part[kPart * blockIdx.x + k] = m;
+      part[kPart * cg::this_cluster().block_rank() + k] = m;
     }
 }
 __device__ __forceinline__ double all_max(const double* part, int k) {
   double m = ldc(part + k);
-  for (int b = 1; b < (int)gridDim.x; ++b) m = dmax(m, ldc(part + kPart * b + k));
+  const int nb = (int)cg::this_cluster().num_blocks();
+  for (int b = 1; b < nb; ++b) m = dmax(m, ldc(part + kPart * b + k));
   return m;
 }
 
@@ -370,9 +372,10 @@ __device__ void energy_and_residual(const SimpleDev& S, bool last, double (&res)
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_simple_steps(SimpleDev S, int nsteps) {
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gstride = gridDim.x * blockDim.x;
+// nsteps time steps of one case on one thread-block cluster
+__device__ void simple_steps(const SimpleDev& S, int nsteps) {
+  const int gtid = (int)cg::this_cluster().block_rank() * blockDim.x + threadIdx.x;
+  const int gstride = (int)cg::this_cluster().num_blocks() * blockDim.x;
   const bool writer = (gtid == 0);
   for (int step = 0; step < nsteps; ++step) {
     for (int it = 0; it < S.n_inner; ++it) {
@@ -423,6 +426,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_simple_steps(SimpleDev S, int n
       // the partials are rewritten only after the next face pass's barrier
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_simple_steps(SimpleDev S, int nsteps) {
+  simple_steps(S, nsteps);
+}
+
+// Independent cases, one cluster each (cluster c runs devs[c]); clusters
+// never wait on one another.
+__global__ void __launch_bounds__(kThreads, 1) k_simple_steps_batch(const SimpleDev* devs,
+                                                                     int nsteps) {
+  __shared__ SimpleDev S;
+  const int c = blockIdx.x / (int)cg::this_cluster().num_blocks();
+  if (threadIdx.x == 0) S = devs[c];
+  __syncthreads();
+  simple_steps(S, nsteps);
 }
 
 // ---- host-side structure -------------------------------------------------------
@@ -820,6 +838,55 @@ mst_status mst_simple_step(mst_simple* s, int nsteps, double* time_rows) {
     S_CU(cudaMemcpyAsync(time_rows, s->time_rows, (size_t)nsteps * 4 * sizeof(double),
                          cudaMemcpyDeviceToHost, s->stream));
   S_CU(cudaStreamSynchronize(s->stream));
+  return MST_OK;
+}
+
+mst_status mst_simple_step_batch(mst_simple* const* cases, int n, int nsteps,
+                                 double* time_rows) {
+  if (!cases || n < 1 || nsteps < 0) return sfail(MST_EINVAL, "bad arguments");
+  for (int i = 0; i < n; ++i)
+    if (!cases[i] || cases[i]->cluster != cases[0]->cluster)
+      return sfail(MST_EINVAL, "NULL case or cases with different cluster sizes");
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (cases[i] == cases[j]) return sfail(MST_EINVAL, "a case is listed twice");
+  if (nsteps == 0) return MST_OK;
+  std::vector<SimpleDev> devs(n);
+  for (int i = 0; i < n; ++i) {
+    if (mst_status st = ensure_rows(cases[i], nsteps)) return st;
+    S_CU(cudaStreamSynchronize(cases[i]->stream));
+    devs[i] = cases[i]->dv;
+  }
+  mst_simple* s0 = cases[0];
+  SimpleDev* d_devs = nullptr;
+  S_CU(cudaMalloc((void**)&d_devs, sizeof(SimpleDev) * n));
+  cudaError_t e = cudaMemcpyAsync(d_devs, devs.data(), sizeof(SimpleDev) * n,
+                                  cudaMemcpyHostToDevice, s0->stream);
+  if (e == cudaSuccess) {
+    cudaFuncSetAttribute(k_simple_steps_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    cfg.gridDim = dim3(s0->cluster * n);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = s0->stream;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = s0->cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_simple_steps_batch, (const SimpleDev*)d_devs, nsteps);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s0->stream);
+  cudaFree(d_devs);
+  if (e != cudaSuccess)
+    return sfail(MST_ECUDA, std::string("mst_simple_step_batch: ") + cudaGetErrorString(e));
+  for (int i = 0; i < n; ++i) {
+    cases[i]->last_steps = nsteps;
+    if (time_rows)
+      S_CU(cudaMemcpy(time_rows + (size_t)4 * nsteps * i, cases[i]->time_rows,
+                      (size_t)nsteps * 4 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return MST_OK;
 }
 

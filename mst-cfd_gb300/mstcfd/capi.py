@@ -254,6 +254,7 @@ def load():
         "mst_simple_get_state": (C.c_int, [C.c_void_p, _dp, _dp]),
         "mst_simple_step": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "mst_simple_rows": (C.c_int, [C.c_void_p, _dp, _ip]),
+        "mst_simple_step_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, _dp]),
         "mst_simple_get_info": (C.c_int, [C.c_void_p, C.POINTER(SimpleInfo)]),
         "mst_simple_destroy": (C.c_int, [C.c_void_p]),
         "mst_last_error": (C.c_char_p, []),

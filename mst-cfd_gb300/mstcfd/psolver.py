@@ -114,6 +114,17 @@ class SimpleSolver:
             pass
 
 
+def step_batch(solvers, nsteps=1):
+    """nsteps time steps of several SimpleSolvers in one launch (one
+    thread-block cluster per case); returns their Time rows
+    [n][nsteps][4]."""
+    n = len(solvers)
+    arr = (C.c_void_p * n)(*[s._h for s in solvers])
+    rows = np.zeros((n, max(int(nsteps), 1), 4))
+    capi.check(capi.load().mst_simple_step_batch(arr, n, int(nsteps), capi.dptr(rows)))
+    return rows[:, :nsteps]
+
+
 class PSolver:
     """The reference's PSolver call surface (pSolver/PSolver.h:16-41)."""
 

@@ -190,3 +190,32 @@ def test_simple_rejects_periodic_mesh():
     with pytest.raises(capi.MstError) as e:
         SimpleSolver(mesh)
     assert e.value.status == capi.EUNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_gpu_batch_equals_single_cases():
+    """Several cases in one launch (one cluster each) give each case's own
+    single-launch bits."""
+    from mstcfd.psolver import step_batch
+    cases = []
+    for name in CASES:
+        g = _fixture(name)
+        cases.append((g["path"], g["rand_puvt"], g["init_face"]))
+    from mstcfd import meshgen as mg
+    path = os.path.join(tempfile.mkdtemp(prefix="simple_b_"), "chan.msh")
+    mg.write_msh(path, _channel(40, 30, 8))
+    m = po.read_msh(path)
+    f0 = np.tile(po.q_to_puvt(np.array(po.reference_inlet())[None])[0], (m.n_faces, 1))
+    cases.append((path, None, f0))
+    singles, batch = [], []
+    for path, p0, f0 in cases:
+        a, _ = _gpu_solver(path, p0, f0)
+        b, _ = _gpu_solver(path, p0, f0)
+        singles.append((a, a.step(3)))
+        batch.append(b)
+    rows = step_batch(batch, 3)
+    for i, ((a, ra), b) in enumerate(zip(singles, batch)):
+        assert same(rows[i], ra), i
+        assert same(a.state()[0], b.state()[0]) and same(a.state()[1], b.state()[1]), i
+        ia, ib = a.rows(), b.rows()
+        assert same(ia[0], ib[0]) and np.array_equal(ia[1], ib[1]), i
