@@ -745,7 +745,8 @@ def run_simple(args, grp):
     out["batch"] = {"cases": n_cases, "cells_per_case": solvers[0].n_cells, "steps": steps,
                     "value": round(n_cases * steps * grp.ws / secs, 2),
                     "unit": "case time steps/s", "ms_per_batch_step": round(1e3 * secs / steps, 3),
-                    "gpu_launches": 1, "note": "mst_simple_step_batch: one cluster per case"}
+                    "gpu_launches": 1, "cluster_ctas": solvers[0].info().batch_cluster,
+                    "note": "mst_simple_step_batch: one cluster per case"}
     for s_ in solvers:
         s_.close()
     return out

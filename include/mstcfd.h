@@ -607,7 +607,8 @@ typedef struct mst_simple_info {
   int cluster, threads;               /* launch shape of the step kernel */
   int momentum_levels, pressure_levels; /* Gauss-Seidel sweep levels */
   int last_steps;                     /* steps of the last mst_simple_step */
-  int reserved;
+  int batch_cluster;                  /* CTAs per cluster of the last
+                                         mst_simple_step_batch led by it */
 } mst_simple_info;
 
 /* The reference's CONST.h values: dt = 1/4000, alpha_p = 0.3, n_inner = 5,
@@ -633,10 +634,11 @@ mst_status mst_simple_get_state(mst_simple *s, double *cell_puvt, double *face_p
  * time_rows (nullable) receives [nsteps][4] max |new - old| / old per
  * component (the Time loop's log row).  One kernel launch. */
 mst_status mst_simple_step(mst_simple *s, int nsteps, double *time_rows);
-/* nsteps time steps of n independent cases (same cluster size) in ONE
- * launch, one thread-block cluster per case, so that several cases fill
- * the GPU; each case's results are those of mst_simple_step.  time_rows
- * (nullable): [n][nsteps][4]. */
+/* nsteps time steps of n independent cases in ONE launch, one
+ * thread-block cluster per case, so that several cases fill the GPU; the
+ * cluster size is chosen for the batch (as many cases resident at once as
+ * pays off; results do not depend on it) and each case's results are those
+ * of mst_simple_step.  time_rows (nullable): [n][nsteps][4]. */
 mst_status mst_simple_step_batch(mst_simple *const *cases, int n, int nsteps,
                                  double *time_rows);
 /* Of the last mst_simple_step: the SIMPLE iteration rows

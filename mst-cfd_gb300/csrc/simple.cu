@@ -531,6 +531,7 @@ struct mst_simple {
   int last_steps = 0;
   int m_levels = 0, p_levels = 0;
   std::vector<double> rho_host;
+  int last_batch_cluster = 0;
 };
 
 namespace {
@@ -845,8 +846,7 @@ mst_status mst_simple_step_batch(mst_simple* const* cases, int n, int nsteps,
                                  double* time_rows) {
   if (!cases || n < 1 || nsteps < 0) return sfail(MST_EINVAL, "bad arguments");
   for (int i = 0; i < n; ++i)
-    if (!cases[i] || cases[i]->cluster != cases[0]->cluster)
-      return sfail(MST_EINVAL, "NULL case or cases with different cluster sizes");
+    if (!cases[i]) return sfail(MST_EINVAL, "NULL case");
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < i; ++j)
       if (cases[i] == cases[j]) return sfail(MST_EINVAL, "a case is listed twice");
@@ -862,20 +862,48 @@ mst_status mst_simple_step_batch(mst_simple* const* cases, int n, int nsteps,
   S_CU(cudaMalloc((void**)&d_devs, sizeof(SimpleDev) * n));
   cudaError_t e = cudaMemcpyAsync(d_devs, devs.data(), sizeof(SimpleDev) * n,
                                   cudaMemcpyHostToDevice, s0->stream);
+  // Cluster size for the batch (results do not depend on it): the one that
+  // minimises waves x per-case time, the per-case time taken to fall as
+  // 1/sqrt(CTAs) (measured: 16, 8, 4 CTAs -> 6.5, 8.1, 11.5 ms on 18k cells)
+  int nb_best = s0->cluster;
   if (e == cudaSuccess) {
     cudaFuncSetAttribute(k_simple_steps_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    double best = 1e300;
+    for (int nb : {16, 8, 4, 2, 1}) {
+      cudaLaunchConfig_t q = {};
+      cudaLaunchAttribute qa[1];
+      q.gridDim = dim3(nb * n);
+      q.blockDim = dim3(kThreads);
+      qa[0].id = cudaLaunchAttributeClusterDimension;
+      qa[0].val.clusterDim.x = nb;
+      qa[0].val.clusterDim.y = 1;
+      qa[0].val.clusterDim.z = 1;
+      q.attrs = qa;
+      q.numAttrs = 1;
+      int active = 0;
+      if (cudaOccupancyMaxActiveClusters(&active, k_simple_steps_batch, &q) != cudaSuccess ||
+          active < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      const double cost = (double)((n + active - 1) / active) / std::sqrt((double)nb);
+      if (cost < best * (1 - 1e-9)) best = cost, nb_best = nb;
+    }
+  }
+  if (e == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
-    cfg.gridDim = dim3(s0->cluster * n);
+    cfg.gridDim = dim3(nb_best * n);
     cfg.blockDim = dim3(kThreads);
     cfg.stream = s0->stream;
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = s0->cluster;
+    at[0].val.clusterDim.x = nb_best;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, k_simple_steps_batch, (const SimpleDev*)d_devs, nsteps);
+    s0->last_batch_cluster = nb_best;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s0->stream);
   cudaFree(d_devs);
@@ -913,6 +941,7 @@ mst_status mst_simple_get_info(const mst_simple* s, mst_simple_info* info) {
   info->momentum_levels = s->m_levels;
   info->pressure_levels = s->p_levels;
   info->last_steps = s->last_steps;
+  info->batch_cluster = s->last_batch_cluster;
   return MST_OK;
 }
 

@@ -123,7 +123,8 @@ class SimpleParams(C.Structure):
 class SimpleInfo(C.Structure):
     _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("cluster", C.c_int),
                 ("threads", C.c_int), ("momentum_levels", C.c_int),
-                ("pressure_levels", C.c_int), ("last_steps", C.c_int), ("reserved", C.c_int)]
+                ("pressure_levels", C.c_int), ("last_steps", C.c_int),
+                ("batch_cluster", C.c_int)]
 
 
 class MstError(RuntimeError):
