@@ -272,6 +272,36 @@ __device__ void pressure(const SimpleDev& S, int gtid, int gstride) {
 }
 
 // ---- SparseSolverNUM::solveGS (lusolver/SparseSolverNUM.cpp:214-252) ---------
+// A thread's first row of one sweep level: its first kPre lower entries
+// (column, L / D[column]) and its own RHS
+constexpr int kPre = 4;
+template <int NS>
+struct SweepRow {
+  int row, k0, k1;
+  int c[kPre];
+  double w[kPre];
+  double rr[NS];
+};
+template <int NS>
+__device__ __forceinline__ void sweep_fetch(SweepRow<NS>& p, int l, const int* lev_ptr,
+                                            const int* lev_rows, const int* l_ptr,
+                                            const int* l_col, const double* w,
+                                            double* const* r, const bool* done, int gtid) {
+  const int i = lev_ptr[l] + gtid;
+  p.row = (i < lev_ptr[l + 1]) ? lev_rows[i] : -1;
+  if (p.row < 0) return;
+  p.k0 = l_ptr[p.row];
+  p.k1 = l_ptr[p.row + 1];
+#pragma unroll
+  for (int t = 0; t < kPre; ++t)
+    if (p.k0 + t < p.k1) {
+      p.c[t] = l_col[p.k0 + t];
+      p.w[t] = ldc(w + p.k0 + t);
+    }
+  for (int s = 0; s < NS; ++s)
+    if (!done[s]) p.rr[s] = ldc(r[s] + p.row);
+}
+
 // NS right-hand sides of one matrix; its[s] receives the iterations run.
 template <int NS>
 __device__ void gauss_seidel(const SimpleDev& S, const int* u_ptr, const int* u_col,
@@ -300,21 +330,36 @@ __device__ void gauss_seidel(const SimpleDev& S, const int* u_ptr, const int* u_
         r[s][row] = ldc(b[s] + row) - acc;
       }
     cluster_sync();
-    // forward sweep, level by level (level 0 rows have no lower entries)
+    // forward sweep, level by level (level 0 rows have no lower entries).
+    // A thread's first row of level l+1 (its entries' columns and weights,
+    // and its own RHS, which only its level changes) is fetched while level
+    // l runs; after the barrier only the RHS of earlier rows is loaded.
+    SweepRow<NS> cur, nxt;
+    if (n_levels > 1) sweep_fetch<NS>(cur, 1, lev_ptr, lev_rows, l_ptr, l_col, w, r, done, gtid);
     for (int l = 1; l < n_levels; ++l) {
-      for (int i = lev_ptr[l] + gtid; i < lev_ptr[l + 1]; i += gstride) {
+      if (l + 1 < n_levels)
+        sweep_fetch<NS>(nxt, l + 1, lev_ptr, lev_rows, l_ptr, l_col, w, r, done, gtid);
+      if (cur.row >= 0)
+        for (int s = 0; s < NS; ++s) {
+          if (done[s]) continue;
+          double acc = cur.rr[s];
+#pragma unroll
+          for (int t = 0; t < kPre; ++t)
+            if (cur.k0 + t < cur.k1) acc -= cur.w[t] * ldc(r[s] + cur.c[t]);
+          for (int k = cur.k0 + kPre; k < cur.k1; ++k) acc -= ldc(w + k) * ldc(r[s] + l_col[k]);
+          r[s][cur.row] = acc;
+        }
+      for (int i = lev_ptr[l] + gtid + gstride; i < lev_ptr[l + 1]; i += gstride) {
         const int row = lev_rows[i];
         for (int s = 0; s < NS; ++s) {
           if (done[s]) continue;
           double acc = ldc(r[s] + row);
-          for (int k = l_ptr[row]; k < l_ptr[row + 1]; ++k) {
-            const int c = l_col[k];
-            acc -= ldc(w + k) * ldc(r[s] + c);
-          }
+          for (int k = l_ptr[row]; k < l_ptr[row + 1]; ++k) acc -= ldc(w + k) * ldc(r[s] + l_col[k]);
           r[s][row] = acc;
         }
       }
       cluster_sync();
+      cur = nxt;
     }
     // X = D^-1 RHS and the largest |X - X'| / X
     double m[NS];
