@@ -11,7 +11,9 @@ between steps.
 
 Arms:
   (default)          the CUDA path through the C ABI; value = FP32-flux /
-                     FP64-accumulate Mcell-updates/s with the state resident
+                     float-pair-accumulate Mcell-updates/s (state and
+                     residual sums as unevaluated FP32 pairs, no FP64
+                     instruction) with the state resident
                      in HBM, timed with CUDA events on the context's stream;
                      "fp64" = the same in FP64; "e2e" = FP32 through the
                      public API with the state copied host->device and back
@@ -833,7 +835,7 @@ def main():
     line = {"metric": METRIC, "value": round(fp32["value"], 2), "unit": UNIT,
             "n_gpus": ws, "steps": fp32["steps"], "warmup": args.warmup,
             "ms_per_step": round(fp32["ms_per_step"], 5), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / float-pair accumulate",
             "data": "synthetic", "config": config,
             "fp64": {"value": round(fp64["value"], 2), "unit": UNIT,
                      "ms_per_step": round(fp64["ms_per_step"], 5), "dtype": "f64"},

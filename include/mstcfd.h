@@ -298,9 +298,13 @@ typedef struct mst_norms {
  * (cudaFree synchronises the whole device; a pool may have no room), and
  * loops that must avoid those implicit synchronisations.  The context is
  * created once at set-up (that call does allocate).
+ * The context must use one Euler stage at a fixed dt (MST_TIME_EULER,
+ * MST_DT_FIXED; others: MST_EUNSUPPORTED); any precision, order, limiter
+ * and viscous setting.
  *   q_dev, qnew_dev  [n_cells][4] doubles in the context's device cell order
  *                    (mst_mesh_arrays.cell_perm gives each file cell's row),
- *                    32-byte aligned; q_dev is read, qnew_dev written
+ *                    32-byte aligned; q_dev is read, qnew_dev written; the
+ *                    buffers (r_dev included) must not overlap (MST_EINVAL)
  *   r_dev            optional [n_cells][4] residual output (same order)
  *   norms_dev        optional 10 doubles: linf_change[4], l2_resid[4],
  *                    mass, dt
@@ -308,8 +312,10 @@ typedef struct mst_norms {
  * about 8.1 MiB that every GPU loading the library keeps until exit, so the
  * mesh may have at most 131072 cells (larger meshes: MST_EINVAL).  All calls
  * share that array: calls that overlap on the GPU race and must be
- * serialised by the caller.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
+ * serialised by the caller.  Every call looks up the array's device
+ * address on the current device; the first call on a device is the set-up
+ * (it may load the library's device code), so make it before any stream
+ * capture. 
  * Runs on the context's stream and returns when the outputs are written;
  * the caller must have finished writing q_dev before the call.  On the FP32
  * path the update is done in FP64 on the caller's buffers (mst_solve keeps

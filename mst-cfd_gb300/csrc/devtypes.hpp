@@ -5,6 +5,8 @@
 
 #include <cstdint>
 
+#include "smem_limit.hpp"
+
 namespace mst {
 
 // Mesh arrays in device numbering (see mesh.hpp DevLayout).  Geometry is

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "smem_limit.hpp"
+
 namespace mst {
 
 // Gradient record per cell: [3][5] plus one pad, so that a cell's gradient

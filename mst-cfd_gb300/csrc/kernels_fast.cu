@@ -1,5 +1,7 @@
-// Production kernels: FP64 and FP32 reconstruction/flux with fused
-// multiply-add allowed; state, residual accumulation and norms stay FP64.
+// Production kernels, fused multiply-add allowed: the FP64 path (all FP64)
+// and the FP32 path (FP32 reconstruction and flux; state, residual sums and
+// update as unevaluated FP32 pairs with compensated sums, no FP64
+// instruction except the last stage's norm epilogue).
 #include "devtypes.hpp"
 #include "mesh.hpp"
 #include "physics.cuh"

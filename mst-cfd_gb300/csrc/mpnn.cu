@@ -21,13 +21,9 @@ namespace tc {
 constexpr uint32_t kLBO = 128, kSBO = 1024;
 
 cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t e = ensure_smem_limit(k_gemm_bf16, kSmemBytes, attr_done);
+  if (e != cudaSuccess) return e;
   GemmArgs a = a0;
   if (a.lbo == 0) {
     a.lbo = kLBO;

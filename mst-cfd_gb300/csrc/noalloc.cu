@@ -24,7 +24,6 @@
 // before reading it, so nothing carries over from the previous call.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "ctx.hpp"
@@ -38,34 +37,26 @@ constexpr size_t kPartBytes = (size_t)kMaxTiles * mst::kNormSlots * sizeof(doubl
 
 static __device__ __align__(256) unsigned char g_scratch[kGradBytes + kPartBytes];
 
-// Host-side handle of g_scratch per device.  In host code the name
-// g_scratch is only a stand-in, not a device address: the address is
-// fetched with cudaGetSymbolAddress, once per device, with that device
-// current, on the first call made on it.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
+// Device address of g_scratch on the current device.  In host code the
+// name g_scratch is only a stand-in, not a device address, so the address
+// is looked up with cudaGetSymbolAddress with the device current.  The
+// first call on a device is the set-up: it may load the library's device
+// code onto that device, so it should come before any stream capture.
+// The lookup is repeated on every call (it allocates nothing once the code
+// is loaded), so an address never outlives a device reset.
 mst_status scratch_for_current_device(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    return mst_internal_fail(MST_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess || !p) {
+    return mst_internal_fail(MST_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    return mst_internal_fail(MST_EUNSUPPORTED, "device index out of range for the scratch table");
-  }
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) {
-      return mst_internal_fail(MST_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    }
-    g_addr[dev] = p;
-  }
-  *out = g_addr[dev];
+  *out = p;
   return MST_OK;
+}
+
+bool overlaps(const void* a, const void* b, size_t n) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  return x < y + n && y < x + n;
 }
 
 // linf[4] (max), l2[4] (sqrt of mean), mass (sum) from the per-tile partials;
@@ -107,6 +98,17 @@ extern "C" mst_status mst_solve_device_noalloc(mst_ctx* c, const double* q_dev,
   if (nC > kMaxCells) {
     return mst_internal_fail(MST_EINVAL, "mst_solve_device_noalloc: mesh has " + std::to_string(nC) +
             " cells; the built-in scratch holds at most " + std::to_string(kMaxCells));
+  }
+  if (c->p.time_scheme != MST_TIME_EULER || c->p.dt_mode != MST_DT_FIXED) {
+    return mst_internal_fail(MST_EUNSUPPORTED, "mst_solve_device_noalloc: the context must use "
+                             "one Euler stage at a fixed dt (time_scheme MST_TIME_EULER, dt_mode "
+                             "MST_DT_FIXED)");
+  }
+  const size_t bytes = (size_t)nC * 4 * sizeof(double);
+  if (overlaps(q_dev, qnew_dev, bytes) || (r_dev && (overlaps(q_dev, r_dev, bytes) ||
+                                                     overlaps(qnew_dev, r_dev, bytes)))) {
+    return mst_internal_fail(MST_EINVAL, "mst_solve_device_noalloc: q_dev, qnew_dev and r_dev "
+                             "must not overlap");
   }
   auto misaligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31) != 0; };
   if (misaligned(q_dev) || misaligned(qnew_dev) || (r_dev && misaligned(r_dev))) {

@@ -13,7 +13,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmstoracle.so")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("MSTCFD_REF_SRC", "/root/reference/MST-CFD")
+# The reference checkout this build recipe compiles from: MSTCFD_REF_SRC,
+# else the build container's read-only copy (absent on GPU machines, where
+# build_ref() is a no-op).  The only place a path of the reference is named.
+REF_SRC = os.environ.get("MSTCFD_REF_SRC") or "/root/reference/MST-CFD"
 
 _SOURCES = ["mstoracle.c", "mstoracle_ext.c", "mstoracle_lu.c", "mstoracle_io.c",
             "mstoracle_simple.c",

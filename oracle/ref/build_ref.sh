@@ -2,8 +2,8 @@
 # Builds the reference oracle (test infrastructure only) into oracle/_ref.
 #
 # The reference's density-based path is compiled from its own sources where
-# they lie (MSTCFD_REF_SRC, default the read-only reference checkout); nothing
-# is copied.  Per variant, oracle/_ref/<variant>/src is a mirror of the
+# they lie (MSTCFD_REF_SRC, required: the read-only reference checkout);
+# nothing is copied.  Per variant, oracle/_ref/<variant>/src is a mirror of the
 # reference tree made of symlinks, plus
 #   * case-fixing symlinks for the includes the sources spell differently
 #     from the file names (sparseSolverNUM.h, sparseSolver.h/.cpp, solverRoe.h),
@@ -17,7 +17,7 @@
 set -euo pipefail
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=${MSTCFD_REF_OUT:-$HERE/../_ref}
-REF=${MSTCFD_REF_SRC:-/root/reference/MST-CFD}
+REF=${MSTCFD_REF_SRC:?set MSTCFD_REF_SRC to the reference MST-CFD source directory}
 THREADS=${MSTCFD_REF_THREADS:-$(nproc)}
 CXX=${CXX:-g++}
 CXXFLAGS="-std=c++20 -O2 -fopenmp -ffp-contract=off -w -I$HERE/eigen_shim"

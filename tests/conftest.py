@@ -10,7 +10,13 @@ for p in (ROOT, PKG):
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_MSH_DIR = "/root/reference/MST-CFD/msh"
+
+def _ref_msh_dir():
+    from oracle import build
+    return os.path.join(build.REF_SRC, "msh")
+
+
+REF_MSH_DIR = _ref_msh_dir()
 
 
 def pytest_configure(config):

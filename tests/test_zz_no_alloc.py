@@ -41,6 +41,7 @@ def _cudart():
         rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
         rt.cudaFree.argtypes = [C.c_void_p]
         rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         return rt
     pytest.fail("CUDA runtime library not found")
 
@@ -67,11 +68,30 @@ class _DevBuf:
         self.rt.cudaFree(self.p)
 
 
-@pytest.mark.parametrize("order", [1, 2])
-@pytest.mark.parametrize("prec", [0, 2], ids=["fp64_exact", "fp32"])
-def test_noalloc_matches_existing_entry_points(order, prec):
+_VISC = dict(viscous=1, mu=0.02, lambda_=-2.0 / 3.0 * 0.02, kappa=0.03, cv=2.5)
+_CASES = {
+    "fp64_exact-o1": (0, 1, {}),
+    "fp64_exact-o2": (0, 2, {}),
+    "fp32-o1": (2, 1, {}),
+    "fp32-o2": (2, 2, {}),
+    "fp64-o2": (1, 2, {}),
+    "fp64-minmod": (1, 2, dict(limiter=1, reference_quirks=0)),
+    "fp64_exact-vanleer-viscous": (0, 2, dict(limiter=2, reference_quirks=0, **_VISC)),
+    "fp32-vanleer-viscous": (2, 2, dict(limiter=2, reference_quirks=0, **_VISC)),
+}
+
+
+def _free_bytes(rt):
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+@pytest.mark.parametrize("case", list(_CASES))
+def test_noalloc_matches_existing_entry_points(case):
     from mstcfd import Mesh, Solver, capi
     from mstcfd import meshgen as mg
+    prec, order, kw = _CASES[case]
     m = mg.reorient(mg.tri_box(60, 30, 4.0, 2.0, jitter=0.25, seed=44), "random", seed=2)
     if order == 2:
         m = mg.with_zone_types(m, mg.OUTLET, mg.WALL)
@@ -79,7 +99,7 @@ def test_noalloc_matches_existing_entry_points(order, prec):
                             m["n_cells"])
     arrs = mesh.arrays()
     q0 = mg.smooth_state(arrs["cell_ctr"])
-    s = Solver(mesh, order=order, precision=prec, dt=2e-4)
+    s = Solver(mesh, order=order, precision=prec, dt=2e-4, **kw)
     # existing entry points
     s.set_state(q0)
     s.solve()
@@ -98,12 +118,16 @@ def test_noalloc_matches_existing_entry_points(order, prec):
         bq.put(q_dev_order)
         lib = capi.load()
         for call in range(2):
+            free0 = _free_bytes(rt)
             st = lib.mst_solve_device_noalloc(s._h, bq.p, bqn.p, br.p, bn.p)
             assert st == capi.OK, lib.mst_last_error()
+            if call == 1:
+                # the point of the entry point: no device memory taken by the call
+                assert _free_bytes(rt) == free0
             qn = bqn.get((nC, 4))[perm]
             r = br.get((nC, 4))[perm]
             nrm = bn.get(10)
-            if prec == 0:
+            if prec in (0, 1):
                 assert np.array_equal(qn, want_qn), call
                 assert np.array_equal(r, want_r), call
                 assert np.array_equal(nrm[:4], want_norms["linf_change"]), call
@@ -142,3 +166,32 @@ def test_noalloc_rejects_meshes_over_the_limit():
     finally:
         b.free()
         s.close()
+
+
+def test_noalloc_rejects_overlap_and_multi_stage_contexts():
+    from mstcfd import Mesh, Solver, capi
+    from mstcfd import meshgen as mg
+    m = mg.tri_box(20, 10, 4.0, 2.0, jitter=0.2, seed=6)
+    mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                            m["n_cells"])
+    rt = _cudart()
+    nb = mesh.n_cells * 32
+    b = _DevBuf(rt, 3 * nb)
+    lib = capi.load()
+    try:
+        s = Solver(mesh, dt=1e-4)
+        q = b.p.value
+        # the new state may not alias the input, nor the residual either one
+        assert lib.mst_solve_device_noalloc(s._h, q, q, None, None) == capi.EINVAL
+        assert b"must not overlap" in lib.mst_last_error()
+        assert lib.mst_solve_device_noalloc(s._h, q, q + nb, q + 32, None) == capi.EINVAL
+        assert lib.mst_solve_device_noalloc(s._h, q, q + nb, q + 2 * nb, None) == capi.OK
+        s.close()
+        # two RK stages or a CFL step are not what one call does: refused
+        for kw in (dict(time_scheme=1), dict(dt_mode=1, cfl=0.5)):
+            s = Solver(mesh, dt=1e-4, **kw)
+            st = lib.mst_solve_device_noalloc(s._h, q, q + nb, None, None)
+            assert st == capi.EUNSUPPORTED, kw
+            s.close()
+    finally:
+        b.free()
