@@ -332,6 +332,20 @@ mst_status mst_solve_device_noalloc(mst_ctx *c, const double *q_dev,
  * finite (the state left the physical range). */
 mst_status mst_step(mst_ctx *c, int nsteps, double t_end, mst_norms *last);
 
+/* Host-held states stepped through the device with the copies hidden
+ * behind the computation (the reference's time loop keeps its state on the
+ * host and hands it to the solver every step, Time.cpp:54-80): job j
+ * copies q_in[j] ([n_cells][4] doubles, file order) to the device, takes
+ * nsteps steps of the configured scheme from it, and copies the result to
+ * q_out[j].  The copy-in of job j+1 and the copy-out of job j-1 run on
+ * their own streams while job j computes (two staging slots each way,
+ * allocated on the first call).  Use page-locked host buffers
+ * (mst_host_alloc) for full-speed copies.  Returns when every q_out is
+ * written; the context's state is then the last job's result.
+ * MST_EDIVERGED when a job's last-step residual or mass is not finite. */
+mst_status mst_step_host_jobs(mst_ctx *c, int n_jobs, const double *const *q_in,
+                              double *const *q_out, int nsteps);
+
 /* Simulated time of the context (sum of the steps taken). */
 mst_status mst_get_time(mst_ctx *c, double *t);
 
@@ -366,12 +380,12 @@ typedef struct mst_implicit_params {
   double omega;     /* LU-SGS relaxation of the spectral radii (>= 1) */
   double tol;       /* a case has converged when L2 <= tol * L2_first; its
                      * state is kept from then on */
-  /* limiter freezing: once a case is below freeze_tol * L2_first and its L2
-   * fell by less than 30% over the last 50 iterations, the next iteration
-   * records the ratio slope / (upwind difference) of every limited face
-   * side; later iterations reconstruct with those ratios times the current
-   * upwind differences, so the limiter's switching no longer stalls
-   * convergence (0: never).  Every update is halved (at most 6 times, else
+  /* limiter freezing (default 0.1): once a case is below freeze_tol *
+   * L2_first and its L2 fell by less than 30% over the last 50
+   * iterations, the next iteration records the ratio slope / (upwind
+   * difference) of every limited face side; later iterations reconstruct
+   * with those ratios times the current upwind differences, so the
+   * limiter's switching no longer stalls convergence (0: never).  Every update is halved (at most 6 times, else
    * dropped) until density and pressure stay above a fifth of their
    * current values. */
   double freeze_tol;
@@ -417,6 +431,7 @@ typedef struct mst_batch_result {
   int total_iterations;  /* since the state was set */
   int n_converged;       /* cases at tolerance */
   double ms;             /* device time of the call */
+  int n_diverged;        /* cases retired as diverged (MST_CASE_DIVERGED) */
 } mst_batch_result;
 
 /* Joins the meshes into one device mesh (cases keep their cells together)
@@ -444,8 +459,12 @@ mst_status mst_batch_get_state(mst_batch *b, double *q);
 mst_status mst_batch_iterate(mst_batch *b, int n);
 /* Iterates until every case has converged or max_iter iterations ran. */
 mst_status mst_batch_solve(mst_batch *b, mst_batch_result *res);
-/* Per case: the iteration at which it converged (-1: not yet), the first
- * and the latest L2 (each nullable). */
+/* Per case: the iteration at which it converged (-1: not yet;
+ * MST_CASE_DIVERGED: retired because its L2 stopped being finite, which a
+ * non-positive density or pressure causes through the sound speed; its
+ * cells cost nothing from the next iteration on and the other cases run
+ * on), the first and the latest L2 (each nullable). */
+enum { MST_CASE_DIVERGED = -2 };
 mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
                                  double *first_l2, double *last_l2);
 
@@ -463,6 +482,15 @@ mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
 mst_status mst_tc_gemm_check(const uint16_t *A, const uint16_t *B,
                              const float *bias, float *C, int M, int N, int K,
                              int relu, int layout);
+
+/* No counterpart in the reference.  Every device-side wait of the
+ * library's kernels (the tensor-core GEMM's mbarrier waits) is bounded:
+ * after `polls` polls it gives up, the kernel finishes its own in-flight
+ * work, frees what it holds and returns, and the call reports
+ * MST_ETIMEOUT; the context stays usable.  polls < 0 restores the default
+ * (2^26); 0 makes every such wait give up at once, which tests the timeout
+ * path without a hang.  Process-wide. */
+mst_status mst_set_wait_limit(long long polls);
 
 /* ------------------------------------------------------------------ */
 /* learned initial field                                                */
@@ -676,6 +704,12 @@ mst_status mst_host_free(void *p);
 mst_status mst_device_count(int *n);
 /* Selects the device later contexts of this host thread are created on. */
 mst_status mst_set_device(int device);
+
+/* Measurement helper, no counterpart in the reference: the current
+ * device's rate of FP64 fused multiply-adds (thread instructions per
+ * second; 2 flops each), from a kernel of independent DFMA chains timed
+ * with CUDA events.  The roof of the FP64-pipe-bound kernels. */
+mst_status mst_probe_fp64_rate(double *dfma_per_s);
 
 /* Text of the last error on this thread (static storage). */
 const char *mst_last_error(void);

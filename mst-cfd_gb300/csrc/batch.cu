@@ -40,11 +40,13 @@ __global__ void k_batch_gather(const double4_32a* __restrict__ src,
   if (i < n) dst[i] = src[idx[i]];
 }
 __global__ void k_batch_reset(int n_cases, double cfl0, double* cfl, int* conv_iter,
-                              int* frozen, double* l2_win, int* n_conv, int* iter) {
+                              int* diverged, int* frozen, double* l2_win, int* n_conv,
+                              int* iter) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_cases) {
     cfl[i] = cfl0;
     conv_iter[i] = -1;
+    diverged[i] = 0;
     frozen[i] = 0;
     l2_win[i] = 0.0;
   }
@@ -73,6 +75,7 @@ struct mst_batch {
   float* case_tab_f = nullptr;
   double *cfl = nullptr, *first = nullptr, *last = nullptr;
   int *conv_iter = nullptr, *n_conv = nullptr, *iter = nullptr;
+  int* diverged = nullptr;       // per case: retired with a non-finite L2
   int* frozen = nullptr;         // per-case limiter-freezing state
   double* l2_win = nullptr;      // per-case L2 at the last freezing check
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
@@ -183,6 +186,7 @@ mst::LusgsArgs sweep_args(mst_batch* b, int which) {
   la.conv_iter = b->conv_iter;
   la.iter = b->iter;
   la.p_floor = b->ip.p_floor;
+  la.case_bad = b->diverged;
   if (b->sweep32) {
     la.qf = qfbuf(b, which);
     la.dqf = b->dqf;
@@ -227,6 +231,7 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.cfl = b->cfl;
   na.conv_iter = b->conv_iter;
   na.n_conv = b->n_conv;
+  na.diverged = b->diverged;
   na.iter = b->iter;
   // the limiter-freezing state machine runs in the FP64 phase only
   na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
@@ -312,7 +317,8 @@ mst_status build_graph(mst_batch* b, int k) {
 
 mst_status reset_progress(mst_batch* b) {
   k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, b->ctx->stream>>>(
-      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->frozen, b->l2_win, b->n_conv, b->iter);
+      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->diverged, b->frozen, b->l2_win,
+      b->n_conv, b->iter);
   B_CU(cudaGetLastError());
   return MST_OK;
 }
@@ -337,7 +343,7 @@ void mst_implicit_params_default(mst_implicit_params* p) {
   p->cfl_max = 100.0;
   p->omega = 1.2;
   p->tol = 1e-8;
-  p->freeze_tol = 1e-2;
+  p->freeze_tol = 1e-1;
   p->max_iter = 20000;
   p->graph_iters = 20;
   p->autotune = 1;
@@ -440,6 +446,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->first, sizeof(double) * n_cases)) ||
       (st = balloc(b.get(), &b->last, sizeof(double) * n_cases)) ||
       (st = balloc(b.get(), &b->conv_iter, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->diverged, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->n_conv, sizeof(int))) ||
       (st = balloc(b.get(), &b->iter, sizeof(int))) ||
       (st = balloc(b.get(), &b->frozen, sizeof(int) * n_cases)) ||
@@ -656,10 +663,15 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   float ms = 0.f;
   B_CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   if (res) {
+    std::vector<int> dv(b->n_cases);
+    B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * dv.size(), cudaMemcpyDeviceToHost));
+    int n_div = 0;
+    for (int x : dv) n_div += x != 0;
     res->iterations = iters;
     res->total_iterations = start + iters;
-    res->n_converged = done;
+    res->n_converged = done - n_div;
     res->ms = ms;
+    res->n_diverged = n_div;
   }
   return MST_OK;
 }
@@ -668,7 +680,13 @@ mst_status mst_batch_case_status(mst_batch* b, int* conv_iter, double* first_l2,
                                  double* last_l2) {
   if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
   const size_t n = (size_t)b->n_cases;
-  if (conv_iter) B_CU(cudaMemcpy(conv_iter, b->conv_iter, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (conv_iter) {
+    std::vector<int> dv(n);
+    B_CU(cudaMemcpy(conv_iter, b->conv_iter, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i)
+      if (dv[i]) conv_iter[i] = MST_CASE_DIVERGED;
+  }
   if (first_l2) B_CU(cudaMemcpy(first_l2, b->first, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (last_l2) B_CU(cudaMemcpy(last_l2, b->last, sizeof(double) * n, cudaMemcpyDeviceToHost));
   return MST_OK;

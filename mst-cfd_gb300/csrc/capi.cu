@@ -23,6 +23,8 @@ namespace {
 
 thread_local std::string g_err;
 
+void release_pipe(mst_ctx* c);  // the host-buffer pipeline's streams and slots
+
 mst_status fail(mst_status s, const std::string& msg) {
   g_err = msg;
   return s;
@@ -446,6 +448,31 @@ mst_status download_rows(mst_ctx* c, const double4_32a* dev, double* host,
 
 mst_status mst_internal_fail(mst_status s, const std::string& msg) { return fail(s, msg); }
 
+namespace {
+
+// FP64 pipe probe: every thread runs 8 independent fused multiply-add
+// chains (x <- x a + b), enough independent work per SM to keep the FP64
+// pipe issuing every cycle it can.  With a = 1 - 2^-20 and b small the
+// values stay bounded.  The sum is stored so nothing is optimised away.
+constexpr int kProbeChains = 8;
+__global__ void __launch_bounds__(256) k_probe_dfma(double a, double b, int iters,
+                                                    double* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double x[kProbeChains];
+#pragma unroll
+  for (int k = 0; k < kProbeChains; ++k) x[k] = 1e-3 * (t & 255) + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < kProbeChains; ++k) s += x[k];
+  out[t] = s;
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 extern "C" {
 
@@ -790,6 +817,7 @@ mst_status mst_ctx_destroy(mst_ctx* c) {
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  release_pipe(c);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MST_OK;
@@ -966,14 +994,17 @@ mst_status mst_get_gradient(mst_ctx* c, double* g) {
   return MST_OK;
 }
 
-mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
-  if (!c) return fail(MST_EINVAL, "NULL context");
-  if (nsteps < 0) return fail(MST_EINVAL, "nsteps must be >= 0");
-  c->last_launches = 0;
-  CU(cudaEventRecord(c->ev0, c->stream));
+}  // extern "C"
+
+namespace {
+
+// nsteps steps of the configured scheme enqueued on the context's stream
+// (no host synchronisation); norms of the last step into c->norms when
+// last_norms is set
+mst_status enqueue_steps(mst_ctx* c, int nsteps, double t_end, bool last_norms = true) {
   for (int s = 0; s < nsteps; ++s) {
     // norms (per-tile partials + one reduction) on the last step only
-    const bool norms = (s == nsteps - 1);
+    const bool norms = last_norms && (s == nsteps - 1);
     bool grad_ready = false;
     mst_status st = compute_dt(c, c->q_old, t_end, c->qf_old, &grad_ready);
     if (st) return st;
@@ -1008,6 +1039,154 @@ mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
     std::swap(c->q_old, c->q_new);
     std::swap(c->qf_old, c->qf_new);
     std::swap(c->ql_old, c->ql_new);
+  }
+  return MST_OK;
+}
+
+// ---- host-buffer pipeline ----
+__global__ void k_load_rows(const double4_32a* __restrict__ src, const int* __restrict__ iperm,
+                            double4_32a* __restrict__ q, float4* __restrict__ hi,
+                            float4* __restrict__ lo, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a v = src[iperm[i]];
+  if (q) q[i] = v;
+  if (hi) {
+    const float4 h = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+    hi[i] = h;
+    lo[i] = make_float4((float)(v.x - (double)h.x), (float)(v.y - (double)h.y),
+                        (float)(v.z - (double)h.z), (float)(v.w - (double)h.w));
+  }
+}
+
+void release_pipe(mst_ctx* c) {
+  mst_ctx::HostPipe& P = c->pipe;
+  if (P.in) cudaStreamSynchronize(P.in);
+  if (P.out) cudaStreamSynchronize(P.out);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(P.slot_in[k]);
+    cudaFree(P.slot_out[k]);
+    for (cudaEvent_t e : {P.in_ready[k], P.in_free[k], P.out_ready[k], P.out_free[k]})
+      if (e) cudaEventDestroy(e);
+  }
+  cudaFree(P.job_norms);
+  if (P.in) cudaStreamDestroy(P.in);
+  if (P.out) cudaStreamDestroy(P.out);
+  P = mst_ctx::HostPipe{};
+}
+
+mst_status ensure_pipe(mst_ctx* c, int n_jobs) {
+  mst_ctx::HostPipe& P = c->pipe;
+  const size_t qbytes = (size_t)c->dm.n_cells * sizeof(double4_32a);
+  if (!P.in) {
+    CU(cudaStreamCreateWithFlags(&P.in, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&P.out, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CU(cudaMalloc((void**)&P.slot_in[k], std::max<size_t>(qbytes, 256)));
+      CU(cudaMalloc((void**)&P.slot_out[k], std::max<size_t>(qbytes, 256)));
+      for (cudaEvent_t* e : {&P.in_ready[k], &P.in_free[k], &P.out_ready[k], &P.out_free[k]})
+        CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+  }
+  if (n_jobs > P.cap) {
+    cudaFree(P.job_norms);
+    P.job_norms = nullptr;
+    P.cap = 0;
+    CU(cudaMalloc((void**)&P.job_norms, sizeof(double) * (kNormSlots + 2) * (size_t)n_jobs));
+    P.cap = n_jobs;
+  }
+  return MST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mst_status mst_step_host_jobs(mst_ctx* c, int n_jobs, const double* const* q_in,
+                              double* const* q_out, int nsteps) {
+  if (!c || n_jobs < 0 || nsteps < 1 || (n_jobs > 0 && (!q_in || !q_out)))
+    return fail(MST_EINVAL, "NULL argument, n_jobs < 0 or nsteps < 1");
+  for (int j = 0; j < n_jobs; ++j)
+    if (!q_in[j] || !q_out[j]) return fail(MST_EINVAL, "NULL job buffer");
+  if (n_jobs == 0) return MST_OK;
+  mst_status st = ensure_pipe(c, n_jobs);
+  if (st) return st;
+  mst_ctx::HostPipe& P = c->pipe;
+  const int nC = c->dm.n_cells;
+  const size_t qbytes = (size_t)nC * sizeof(double4_32a);
+  const int nb = (nC + 255) / 256;
+  const bool fp32 = pairs(c);
+  c->last_launches = 0;
+  CU(cudaEventRecord(c->ev0, c->stream));
+  // no slot is in use before the first jobs
+  for (int k = 0; k < 2; ++k) {
+    CU(cudaEventRecord(P.in_free[k], c->stream));
+    CU(cudaEventRecord(P.out_free[k], P.out));
+  }
+  for (int j = 0; j < n_jobs; ++j) {
+    const int k = j & 1;
+    // in: host -> slot (after the slot's previous job was loaded)
+    CU(cudaStreamWaitEvent(P.in, P.in_free[k], 0));
+    CU(cudaMemcpyAsync(P.slot_in[k], q_in[j], qbytes, cudaMemcpyHostToDevice, P.in));
+    CU(cudaEventRecord(P.in_ready[k], P.in));
+    // compute: slot -> state (device order; float pairs on the FP32 path)
+    CU(cudaStreamWaitEvent(c->stream, P.in_ready[k], 0));
+    k_load_rows<<<nb, 256, 0, c->stream>>>(P.slot_in[k], c->d.cell_iperm,
+                                            fp32 ? nullptr : c->q_old,
+                                            fp32 ? c->qf_old : nullptr,
+                                            fp32 ? c->ql_old : nullptr, nC);
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(P.in_free[k], c->stream));
+    c->grad_valid = false;
+    st = enqueue_steps(c, nsteps, 0.0);
+    if (st) return st;
+    CU(cudaMemcpyAsync(P.job_norms + (size_t)j * (kNormSlots + 2), c->norms,
+                       sizeof(double) * (kNormSlots + 2), cudaMemcpyDeviceToDevice, c->stream));
+    // state -> out slot in file order (after the slot's previous job left)
+    CU(cudaStreamWaitEvent(c->stream, P.out_free[k], 0));
+    if (fp32)
+      k_from_pairs<<<nb, 256, 0, c->stream>>>(c->qf_old, c->ql_old, c->d.cell_perm,
+                                               P.slot_out[k], nC);
+    else
+      k_gather_rows<<<nb, 256, 0, c->stream>>>(c->q_old, c->d.cell_perm, P.slot_out[k], nC);
+    CU(cudaGetLastError());
+    c->last_launches += 2;
+    CU(cudaEventRecord(P.out_ready[k], c->stream));
+    // out: slot -> host
+    CU(cudaStreamWaitEvent(P.out, P.out_ready[k], 0));
+    CU(cudaMemcpyAsync(q_out[j], P.slot_out[k], qbytes, cudaMemcpyDeviceToHost, P.out));
+    CU(cudaEventRecord(P.out_free[k], P.out));
+  }
+  CU(cudaEventRecord(c->ev1, P.out));
+  c->timed = true;
+  CU(cudaStreamSynchronize(P.out));
+  CU(cudaStreamSynchronize(c->stream));
+  drain_profile(c);
+  // the context's state is the last job's result; every job's last-step
+  // norms decide divergence as in mst_step
+  std::vector<double> h((size_t)n_jobs * (kNormSlots + 2));
+  CU(cudaMemcpy(h.data(), P.job_norms, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+  if (c->volumes_ok) {
+    for (int j = 0; j < n_jobs; ++j) {
+      const double* n = h.data() + (size_t)j * (kNormSlots + 2);
+      bool finite = std::isfinite(n[8]);
+      for (int q = 4; q < 8; ++q) finite = finite && std::isfinite(n[q]);
+      if (!finite)
+        return fail(MST_EDIVERGED, "mst_step_host_jobs: job " + std::to_string(j) +
+                                       ": the residual or the mass is not finite");
+    }
+  }
+  return MST_OK;
+}
+
+mst_status mst_step(mst_ctx* c, int nsteps, double t_end, mst_norms* last) {
+  if (!c) return fail(MST_EINVAL, "NULL context");
+  if (nsteps < 0) return fail(MST_EINVAL, "nsteps must be >= 0");
+  c->last_launches = 0;
+  CU(cudaEventRecord(c->ev0, c->stream));
+  {
+    mst_status st = enqueue_steps(c, nsteps, t_end);
+    if (st) return st;
   }
   CU(cudaEventRecord(c->ev1, c->stream));
   c->timed = true;
@@ -1097,6 +1276,39 @@ mst_status mst_device_count(int* n) {
     *n = 0;
     return fail(MST_ECUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
   }
+  return MST_OK;
+}
+
+mst_status mst_probe_fp64_rate(double* dfma_per_s) {
+  if (!dfma_per_s) return fail(MST_EINVAL, "NULL argument");
+  *dfma_per_s = 0.0;
+  int dev = 0, sms = 0;
+  CU(cudaGetDevice(&dev));
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  double* out = nullptr;
+  CU(cudaMalloc((void**)&out, sizeof(double) * (size_t)threads * blocks));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // the first warms up
+    cudaEventRecord(e0, 0);
+    k_probe_dfma<<<blocks, threads>>>(1.0 - 0x1p-20, 1e-9, iters, out);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return fail(MST_ECUDA, std::string("fp64 probe: ") + cudaGetErrorString(e));
+  if (!(best > 0.f)) return fail(MST_ECUDA, "fp64 probe: no timing");
+  *dfma_per_s = (double)threads * blocks * iters * kProbeChains / (best * 1e-3);
   return MST_OK;
 }
 

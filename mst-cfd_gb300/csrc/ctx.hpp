@@ -84,5 +84,15 @@ struct mst_ctx {
   bool volumes_ok = true;
   std::vector<void*> allocs;
   mst_node_avg* node_avg = nullptr;
+  // host-buffer pipeline (mst_step_host_jobs): copy-in and copy-out
+  // streams, two staging slots each way, and the norms of every job
+  struct HostPipe {
+    cudaStream_t in = nullptr, out = nullptr;
+    double4_32a* slot_in[2] = {nullptr, nullptr};
+    double4_32a* slot_out[2] = {nullptr, nullptr};
+    cudaEvent_t in_ready[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
+    double* job_norms = nullptr;  // [cap][kNormSlots + 2], device
+    int cap = 0;
+  } pipe;
 };
 

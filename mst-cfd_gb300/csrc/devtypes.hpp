@@ -155,6 +155,8 @@ struct LusgsArgs {
   const float* case_tab_f;
   float mu_f;
   double p_floor;          // temperature floor p >= p_floor * rho (0: off)
+  int* case_bad;           // [n_cases] set to 1 when a swept state has a
+                           // non-positive (or NaN) density or pressure
 };
 
 // Per-case residual norms and the CFL of the next iteration, one block per
@@ -169,8 +171,10 @@ struct CaseNormArgs {
   double* first;           // [n_cases] L2 of iteration 0
   double* last;            // [n_cases] latest L2
   double* cfl;             // [n_cases]
-  int* conv_iter;          // [n_cases] -1 until converged
-  int* n_conv;             // number of converged cases
+  int* conv_iter;          // [n_cases] -1 until the case is done (converged
+                           // or diverged): the iteration it finished at
+  int* n_conv;             // number of finished cases
+  int* diverged;           // [n_cases] 1 once the case's L2 is not finite
   int* iter;               // iteration counter (advanced by k_iter_advance)
   int* frozen;             // [n_cases] limiter-freezing state (or nullptr)
   double* l2_win;          // [n_cases] L2 at the last freezing-window check

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -20,11 +21,16 @@ namespace tc {
 // dimension), 8-row groups 1024 bytes apart (stride dimension).
 constexpr uint32_t kLBO = 128, kSBO = 1024;
 
+// polls of the GEMM's bounded mbarrier waits (mst_set_wait_limit)
+std::atomic<long long> g_wait_limit{-1};
+
 cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   static std::atomic<uint64_t> attr_done{0};
   cudaError_t e = ensure_smem_limit(k_gemm_bf16, kSmemBytes, attr_done);
   if (e != cudaSuccess) return e;
   GemmArgs a = a0;
+  const long long lim = g_wait_limit.load(std::memory_order_relaxed);
+  a.spin_limit = lim < 0 ? kSpinLimit : (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
   if (a.lbo == 0) {
     a.lbo = kLBO;
     a.sbo = kSBO;
@@ -676,6 +682,11 @@ mst_status mst_mpnn_adam_step(mst_mpnn* m, float lr) {
   return MST_OK;
 }
 
+
+mst_status mst_set_wait_limit(long long polls) {
+  mst::tc::g_wait_limit.store(polls < 0 ? -1 : polls, std::memory_order_relaxed);
+  return MST_OK;
+}
 
 mst_status mst_tc_gemm_check(const uint16_t* A, const uint16_t* B, const float* bias, float* C,
                              int M, int N, int K, int relu, int layout) {

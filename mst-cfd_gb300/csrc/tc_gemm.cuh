@@ -14,8 +14,9 @@
 // per tile and commits them to the stage's mbarrier; a stage is refilled
 // only after that commit has arrived.  The epilogue reads the accumulator
 // with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows) and applies
-// bias / ReLU.  Every mbarrier wait is bounded: on timeout the kernel sets
-// *err, waits (bounded) for its own MMAs, frees its TMEM and returns.
+// bias / ReLU.  Every mbarrier wait is bounded (GemmArgs.spin_limit polls;
+// mst_set_wait_limit): on timeout the kernel sets *err, waits (bounded by
+// the full limit) for its own copies and MMAs, frees its TMEM and returns.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -60,10 +61,12 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
 
-// bounded wait for the phase with the given parity; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// bounded wait for the phase with the given parity (at most `limit` polls);
+// false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned limit = kSpinLimit) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned i = 0; i < kSpinLimit; ++i) {
+  for (unsigned i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -128,6 +131,7 @@ struct GemmArgs {
   int accumulate_c;        // C += result (FP32 output only)
   uint32_t lbo, sbo;       // descriptor strides (bytes)
   int* err;                // set on a timed-out wait
+  unsigned spin_limit;     // polls of each main-loop wait (0: give up at once)
   // split K: CTA z covers K range [z * k_chunk, (z + 1) * k_chunk) and
   // writes its partial product to C + z * M * ldc (no bias / ReLU);
   // k_chunk = 0: one CTA per output tile over the whole K
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
       // stage s1 last held tile t-1: thread 0 waits for its MMAs (bounded)
       // and tells the block, so every thread takes the same branch
       if (t >= 1) {
-        if (tid == 0 && !mbar_wait(&bars[s1], ((t - 1) >> 1) & 1)) *s_ok = 0;
+        if (tid == 0 && !mbar_wait(&bars[s1], ((t - 1) >> 1) & 1, g.spin_limit)) *s_ok = 0;
         __syncthreads();
         ok = *s_ok != 0;
         if (!ok) break;
@@ -223,13 +227,23 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   // the host sizes split-K chunks so that every CTA has a K tile
   if (ok && issued > 0) {
     const int tl = issued - 1;
-    if (tid == 0 && !mbar_wait(&bars[tl & 1], (tl >> 1) & 1)) *s_ok = 0;
+    if (tid == 0 && !mbar_wait(&bars[tl & 1], (tl >> 1) & 1, g.spin_limit)) *s_ok = 0;
   }
   __syncthreads();
   ok = *s_ok != 0;
   if (!ok) {
-    if (tid == 0) atomicExch(g.err, 1);
+    // timed out: report it, then let this CTA's own work finish before the
+    // tensor memory is freed -- its copies, and (thread 0, with the full
+    // limit) the last committed MMAs, whose commit covers all earlier ones
+    if (tid == 0) {
+      atomicExch(g.err, 1);
+      if (issued > 0) {
+        const int tl = issued - 1;
+        mbar_wait(&bars[tl & 1], (tl >> 1) & 1, kSpinLimit);
+      }
+    }
     cp_async_wait<0>();
+    __syncthreads();
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {

@@ -90,7 +90,10 @@ class BatchInfo(C.Structure):
 
 class BatchResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("total_iterations", C.c_int),
-                ("n_converged", C.c_int), ("ms", C.c_double)]
+                ("n_converged", C.c_int), ("ms", C.c_double), ("n_diverged", C.c_int)]
+
+
+CASE_DIVERGED = -2  # mst_batch_case_status: the case was retired as diverged
 
 
 class MeshInfo(C.Structure):
@@ -185,6 +188,10 @@ def load():
         "mst_host_free": (C.c_int, [C.c_void_p]),
         "mst_device_count": (C.c_int, [_ip]),
         "mst_set_device": (C.c_int, [C.c_int]),
+        "mst_probe_fp64_rate": (C.c_int, [_dp]),
+        "mst_set_wait_limit": (C.c_int, [C.c_longlong]),
+        "mst_step_host_jobs": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p),
+                                         C.POINTER(C.c_void_p), C.c_int]),
         "mst_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p]),
         "mst_node_values": (C.c_int, [C.c_void_p, _dp, _dp]),

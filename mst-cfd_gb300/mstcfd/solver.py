@@ -217,6 +217,17 @@ class Solver:
     def get_state_ptr(self, ptr, stride=4):
         capi.check(capi.load().mst_get_state(self._h, C.cast(ptr, capi._dp), stride))
 
+    def step_host_jobs(self, q_in_ptrs, q_out_ptrs, nsteps=1):
+        """Independent host-held states (raw host pointers, [n_cells][4]
+        doubles each; page-locked for full-speed copies) stepped nsteps
+        each, copies overlapped with the computation."""
+        n = len(q_in_ptrs)
+        if len(q_out_ptrs) != n:
+            raise ValueError("one output buffer per input")
+        ins = (C.c_void_p * max(n, 1))(*[int(p) for p in q_in_ptrs])
+        outs = (C.c_void_p * max(n, 1))(*[int(p) for p in q_out_ptrs])
+        capi.check(capi.load().mst_step_host_jobs(self._h, n, ins, outs, int(nsteps)))
+
     def close(self):
         h = getattr(self, "_h", None)
         if h:

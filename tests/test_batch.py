@@ -185,6 +185,44 @@ def test_gpu_batch_solve_converges_and_graph_is_deterministic():
 
 
 @pytest.mark.gpu
+def test_gpu_batch_retires_diverged_cases():
+    """Per-case divergence detection: two cases whose initial state is
+    poisoned on the host (a NaN cell; a cell of negative pressure) are
+    retired as MST_CASE_DIVERGED at their first iteration and cost nothing
+    afterwards, while the healthy cases converge to exactly the states of
+    the same batch without the poisoned ones."""
+    from mstcfd import batch, capi
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    imp = dict(cfl0=50.0, cfl_max=1000.0, omega=1.2, tol=1e-8, freeze_tol=1e-1, max_iter=3000,
+               graph_iters=10)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    bad_nan = q0[0].copy()
+    bad_nan[len(bad_nan) // 2, 0] = np.nan
+    bad_p = q0[1].copy()
+    bad_p[7, 3] = 0.25 * (bad_p[7, 1] ** 2 + bad_p[7, 2] ** 2) / bad_p[7, 0]  # E < kinetic
+    poisoned = [(cases[0][1], cases[0][3]), (cases[1][1], cases[1][3])]
+    all_cases = poisoned + [(mesh, cp) for _, mesh, _, cp in cases]
+    b = batch.Batch(all_cases, implicit=imp, **kw)
+    b.set_state([bad_nan, bad_p] + q0)
+    r = b.solve()
+    st = b.case_status()
+    assert list(st["conv_iter"][:2]) == [capi.CASE_DIVERGED] * 2
+    assert r["n_diverged"] == 2 and r["n_converged"] == len(cases)
+    assert np.all(st["conv_iter"][2:] > 0)
+    got = b.state()[2:]
+    b.close()
+    ref = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    ref.set_state(q0)
+    r2 = ref.solve()
+    assert r2["iterations"] == r["iterations"] and r2["n_diverged"] == 0
+    for a, c in zip(got, ref.state()):
+        assert np.array_equal(a, c)
+    ref.close()
+
+
+@pytest.mark.gpu
 def test_gpu_batch_solve_matches_oracle_solve():
     """FP64-exact batch solved to 1e-8 with limiter freezing: every case's
     final state and convergence iteration equal the oracle's single-case

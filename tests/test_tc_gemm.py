@@ -65,3 +65,24 @@ def test_tc_gemm_split_k(M, N, K, chunk):
     assert st == capi.OK, capi.load().mst_last_error()
     tol = 1e-5 * np.sqrt(K) * (np.abs(ref).max() + 1)
     assert np.abs(got - ref).max() <= tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [64, 256])
+def test_tc_gemm_wait_timeout_reports_and_recovers(K):
+    """A bounded device wait that runs out: with the wait limit at 0 every
+    mbarrier wait of the GEMM gives up at once, the kernel drains its own
+    MMAs, frees its tensor memory and returns, and the call reports
+    MST_ETIMEOUT; with the default limit back the next call is correct."""
+    from mstcfd import capi
+    L = capi.load()
+    try:
+        assert L.mst_set_wait_limit(0) == capi.OK
+        st, _, _ = _run(256, 128, K, 0, 0)
+        assert st == capi.ETIMEOUT
+        assert b"timed out" in L.mst_last_error()
+    finally:
+        L.mst_set_wait_limit(-1)
+    st, got, ref = _run(256, 128, K, 0, 0)
+    assert st == capi.OK, L.mst_last_error()
+    assert np.abs(got - ref).max() <= 1e-5 * np.sqrt(K) * (np.abs(ref).max() + 1)
