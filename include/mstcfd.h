@@ -122,6 +122,10 @@ typedef struct mst_mesh_info {
   int n_nodes, n_cells, n_faces, n_int_faces, n_zones, n_cell_faces;
   int n_inner, n_bond1, n_bond2; /* MshBlock boundary lists (:370-406) */
   int n_tiles;                   /* device cell tiles */
+  /* device layout: faces each tile borrows from another, halo entries over
+   * all tiles, distinct halo cells and their cell-faces (what the FP32
+   * flux kernel reads beyond its own cells when it forms the gradients) */
+  int n_borrowed, n_halo, n_halo_cells, n_halo_cell_faces;
 } mst_mesh_info;
 mst_status mst_mesh_get_info(const mst_mesh *m, mst_mesh_info *info);
 

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -263,7 +264,9 @@ mst_status launch_grad(mst_ctx* c, const double4_32a* q, const float4* qf = null
 }
 
 mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
-  ProfScope ps(c, c->p.precision == MST_PREC_FP32 ? "k_flux_update<f32>" : "k_flux_update<f64>");
+  ProfScope ps(c, c->p.precision != MST_PREC_FP32 ? "k_flux_update<f64>"
+                  : a.tile_grad                   ? "k_flux_update<f32,tg>"
+                                                  : "k_flux_update<f32>");
   cudaError_t e = (c->p.precision == MST_PREC_FP64_EXACT)
                       ? mst::exact::launch_flux_update(prec_of(c->p), c->p.flux, c->p.order,
                                                        c->dm, a, 0, c->stream)
@@ -275,6 +278,18 @@ mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
 }
 
 bool pairs(const mst_ctx* c) { return c->p.precision == MST_PREC_FP32; }
+
+// The FP32 float-pair path at 2nd order in the corrected mode forms its
+// gradients inside the flux kernel (k_flux_update TG: no gradient pass, no
+// gradient through HBM).  MSTCFD_FP32_GRADIENT_PASS=1 in the environment
+// keeps the separate gradient pass instead, to compare the two schedules.
+bool tile_grad(const mst_ctx* c) {
+  static const bool pass = [] {
+    const char* e = std::getenv("MSTCFD_FP32_GRADIENT_PASS");
+    return e && e[0] == '1';
+  }();
+  return pairs(c) && c->p.order == 2 && c->p.reference_quirks == 0 && !pass;
+}
 
 // double copies of the float-pair states (device order) for the entry
 // points that read the FP64 buffers
@@ -323,7 +338,8 @@ mst_status run_stage(mst_ctx* c, const StageBufs& b, int stage, bool fixed_dt, b
   double4_32a* qn = b.qn;
   const float4* qf = pairs(c) ? b.qf : nullptr;
   float4* qfn = pairs(c) ? b.qfn : nullptr;
-  if (c->p.order == 2 && !grad_ready) {
+  const bool tg = tile_grad(c);
+  if (c->p.order == 2 && !grad_ready && !tg) {
     mst_status s = launch_grad(c, q, qf);
     if (s) return s;
   }
@@ -331,6 +347,7 @@ mst_status run_stage(mst_ctx* c, const StageBufs& b, int stage, bool fixed_dt, b
   a.q = q;
   a.qf = qf;
   a.qfn = qfn;
+  a.tile_grad = tg ? 1 : 0;
   if (pairs(c)) {
     a.qlo = b.ql;
     a.qlon = b.qln;
@@ -362,7 +379,16 @@ mst_status compute_dt(mst_ctx* c, const double4_32a* q, double t_end,
                       const float4* qf = nullptr, bool* grad_ready = nullptr) {
   const int nC = c->dm.n_cells;
   int mode = 0;
-  if (c->p.dt_mode != MST_DT_FIXED && c->p.order == 2 && grad_ready) {
+  if (c->p.dt_mode != MST_DT_FIXED && tile_grad(c)) {
+    // no gradient pass on this schedule: the step from the FP32 state alone
+    ProfScope ps(c, "k_cfl_dt_pairs");
+    cudaError_t e = mst::fast::launch_cfl_dt_pairs(
+        c->dm, qf, c->p.cfl, c->p.dt_mode == MST_DT_CFL_LOCAL ? c->dt_cell_ff : nullptr,
+        c->dt_part, c->stream);
+    c->last_launches++;
+    if (e != cudaSuccess) return fail(MST_ECUDA, std::string("cfl_dt: ") + cudaGetErrorString(e));
+    mode = 1;
+  } else if (c->p.dt_mode != MST_DT_FIXED && c->p.order == 2 && grad_ready) {
     mst_status st = launch_grad(c, q, qf, c->dt_part, c->p.dt_mode == MST_DT_CFL_LOCAL);
     if (st) return st;
     *grad_ready = true;
@@ -624,6 +650,10 @@ mst_status mst_mesh_get_info(const mst_mesh* m, mst_mesh_info* info) {
   info->n_bond1 = (int)h.bond1.size();
   info->n_bond2 = (int)h.bond2.size();
   info->n_tiles = m->lay.n_tiles;
+  info->n_borrowed = (int)m->lay.t_bor.size();
+  info->n_halo = (int)m->lay.t_halo.size();
+  info->n_halo_cells = m->lay.n_halo_cells;
+  info->n_halo_cell_faces = m->lay.n_halo_cell_faces;
   return MST_OK;
 }
 
@@ -742,6 +772,10 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
     CU(up(&d.t_own_ptr, L.t_own_ptr));
     CU(up(&d.t_bor_ptr, L.t_bor_ptr));
     CU(up(&d.t_bor, L.t_bor));
+    CU(up(&d.t_halo_ptr, L.t_halo_ptr));
+    CU(up(&d.t_halo, L.t_halo));
+    CU(up(&d.t_slot_loc, L.t_slot_loc));
+    CU(up(&d.cf_nbl, L.cf_nbl));
     CU(up(&d.cell_iperm, L.cell_iperm));
     CU(up(&d.cell_perm, L.cell_perm));
   }
@@ -775,6 +809,11 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.t_own_ptr = d.t_own_ptr;
   dm.t_bor_ptr = d.t_bor_ptr;
   dm.t_bor = d.t_bor;
+  dm.t_halo_ptr = d.t_halo_ptr;
+  dm.t_halo = d.t_halo;
+  dm.t_slot_loc = d.t_slot_loc;
+  dm.cf_nbl = d.cf_nbl;
+  dm.max_halo = L.max_halo;
   const size_t nC = L.n_cells, nB = (nC + 255) / 256;
   const size_t qbytes = nC * sizeof(double4_32a);
   if ((st = dalloc(c.get(), &c->q_old, qbytes)) || (st = dalloc(c.get(), &c->q_new, qbytes)) ||

@@ -40,7 +40,8 @@ struct DevArrays {
   float2* c_ivol_ff = nullptr;
   int *c_ptr = nullptr, *cf_face = nullptr, *cf_slot = nullptr, *cf_nb = nullptr,
       *cf_nb_fix = nullptr, *t_own_ptr = nullptr, *t_bor_ptr = nullptr,
-      *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr;
+      *t_bor = nullptr, *cell_iperm = nullptr, *cell_perm = nullptr,
+      *t_halo_ptr = nullptr, *t_halo = nullptr, *t_slot_loc = nullptr, *cf_nbl = nullptr;
 };
 
 struct mst_node_avg;  // result writer buffers (io.cu)

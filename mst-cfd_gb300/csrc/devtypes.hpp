@@ -40,6 +40,13 @@ struct DevMesh {
   const int* t_own_ptr;
   const int* t_bor_ptr;
   const int* t_bor;
+  // fused FP32 tile pass (mesh.hpp DevLayout): halo cells per tile, local
+  // cell indices of every tile face slot and of every cell-face neighbour
+  const int* t_halo_ptr;
+  const int* t_halo;
+  const int* t_slot_loc;
+  const int* cf_nbl;
+  int max_halo;
   // batches (nullptr for a single mesh): the case of every device cell and
   // the iteration at which each case converged (-1 while it runs).  The
   // residual kernels skip the cells of converged cases: after the
@@ -88,6 +95,8 @@ struct StepArgs {
   double dt;              // fixed step
   int stage;              // 0: Q - dt/V R;  1: 0.5 Q0 + 0.5 (Q - dt/V R)
   int quirks;             // reproduce the reference's quirks
+  int tile_grad;          // FP32 pairs, 2nd order, corrected mode: the flux
+                          // kernel forms the gradients itself (grad unused)
   int limiter;            // MST_LIMITER_*
   double inlet[4];
   int viscous;            // laminar viscous term on
@@ -214,6 +223,9 @@ enum { kFluxAusm = 0, kFluxRoe = 1 };
                               int threads, cudaStream_t s);                   \
   cudaError_t lusgs_backward_t(const DevMesh& m, const LusgsArgs& a,         \
                                int threads, cudaStream_t s);                  \
+  cudaError_t launch_cfl_dt_pairs(const DevMesh& m, const float4* qf,        \
+                                  double cfl, float2* dt_cell_ff,             \
+                                  double* dt_part, cudaStream_t s);           \
   cudaError_t case_norms_t(const DevMesh& m, const CaseNormArgs& a,          \
                            int n_cases, cudaStream_t s);                      \
   }

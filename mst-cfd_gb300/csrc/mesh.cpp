@@ -597,6 +597,86 @@ int build_layout(const HostMesh& m, bool renumber, DevLayout* L,
       }
     }
   }
+  // fused-pass tables: halo cells per tile, local cell indices per face slot
+  // and per cell-face
+  {
+    std::vector<std::vector<int>> halo(nT);
+    for (int i = 0; i < nF; ++i) {
+      const int c1 = m.face_cells[2 * i + 1];
+      if (c1 < 0) continue;
+      const int a = L->cell_perm[m.face_cells[2 * i]], b = L->cell_perm[c1];
+      const int ta = tile_of(a), tb = tile_of(b);
+      if (ta == tb) continue;
+      halo[ta].push_back(b);
+      halo[tb].push_back(a);
+    }
+    L->t_halo_ptr.assign(nT + 1, 0);
+    L->t_halo.clear();
+    L->max_halo = 0;
+    for (int t = 0; t < nT; ++t) {
+      auto& h = halo[t];
+      std::sort(h.begin(), h.end());
+      h.erase(std::unique(h.begin(), h.end()), h.end());
+      L->t_halo.insert(L->t_halo.end(), h.begin(), h.end());
+      L->t_halo_ptr[t + 1] = (int)L->t_halo.size();
+      L->max_halo = std::max(L->max_halo, (int)h.size());
+    }
+    {
+      std::vector<char> in_halo(nC, 0);
+      for (int dc : L->t_halo) in_halo[dc] = 1;
+      L->n_halo_cells = 0;
+      L->n_halo_cell_faces = 0;
+      for (int dc = 0; dc < nC; ++dc)
+        if (in_halo[dc]) {
+          ++L->n_halo_cells;
+          L->n_halo_cell_faces += L->c_ptr[dc + 1] - L->c_ptr[dc];
+        }
+    }
+    if (kTileCells + L->max_halo >= 0xFFFF) {
+      *err = "internal: tile halo too large for 16-bit local indices";
+      return kEInval;
+    }
+    auto local = [&](int t, int dc) -> int {
+      const int cb = t * kTileCells;
+      if (dc >= cb && dc < cb + kTileCells) return dc - cb;
+      const int* b = L->t_halo.data() + L->t_halo_ptr[t];
+      const int* e = L->t_halo.data() + L->t_halo_ptr[t + 1];
+      const int* p = std::lower_bound(b, e, dc);
+      if (p == e || *p != dc) return -1;
+      return kTileCells + (int)(p - b);
+    };
+    L->t_slot_loc.assign((size_t)nF + L->t_bor.size(), 0);
+    for (int t = 0; t < nT; ++t) {
+      const int ob = L->t_own_ptr[t], n_own = L->t_own_ptr[t + 1] - ob;
+      const int bb = L->t_bor_ptr[t], n_bor = L->t_bor_ptr[t + 1] - bb;
+      const size_t base = (size_t)ob + bb;
+      for (int sl = 0; sl < n_own + n_bor; ++sl) {
+        const int df = sl < n_own ? ob + sl : L->t_bor[bb + sl - n_own];
+        const int l0 = local(t, L->f_c0c1[2 * (size_t)df]);
+        const int c1 = L->f_c0c1[2 * (size_t)df + 1];
+        const int l1 = c1 >= 0 ? local(t, c1) : 0xFFFF;
+        if (l0 < 0 || l1 < 0) {
+          *err = "internal: face cell missing from its tile table";
+          return kEInval;
+        }
+        L->t_slot_loc[base + sl] = l0 | (l1 << 16);
+      }
+    }
+    L->cf_nbl.assign(tot, 0);
+    for (int dc = 0; dc < nC; ++dc) {
+      const int t = tile_of(dc);
+      for (int dk = L->c_ptr[dc]; dk < L->c_ptr[dc + 1]; ++dk) {
+        const int nbm = L->cf_nb_fix[dk];
+        const int nb = nbm & ((1 << kFvShift) - 1);
+        const int l = local(t, nb);
+        if (l < 0) {
+          *err = "internal: neighbour missing from its tile table";
+          return kEInval;
+        }
+        L->cf_nbl[dk] = l | ((nbm >> kFvShift) << 16);
+      }
+    }
+  }
   return kOk;
 }
 

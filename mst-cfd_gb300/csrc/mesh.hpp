@@ -141,6 +141,21 @@ struct DevLayout {
   std::vector<int> t_own_ptr;   // [nT+1] owned face range (device ids)
   std::vector<int> t_bor_ptr;   // [nT+1] into t_bor
   std::vector<int> t_bor;       // borrowed device face ids
+  // fused FP32 tile pass (gradients formed in shared memory): per tile a
+  // table of its cells (local 0..kTileCells-1) followed by its halo cells
+  // (outside the tile, sharing an interior face with a tile cell)
+  std::vector<int> t_halo_ptr;  // [nT+1] into t_halo
+  std::vector<int> t_halo;      // halo device cells, ascending per tile
+  std::vector<int> t_slot_loc;  // per tile face slot (tile t's slots start at
+                                // t_own_ptr[t] + t_bor_ptr[t]): local index
+                                // of c0 | local index of c1 << 16 (0xFFFF:
+                                // boundary face)
+  std::vector<int> cf_nbl;      // [tot] local index of the neighbour in its
+                                // cell's tile table | corrected face-value
+                                // mode << 16
+  int max_halo = 0;
+  int n_halo_cells = 0;       // distinct cells in some tile's halo
+  int n_halo_cell_faces = 0;  // their cell-faces
 };
 
 int build_layout(const HostMesh& m, bool renumber, DevLayout* L,

@@ -99,7 +99,8 @@ CASE_DIVERGED = -2  # mst_batch_case_status: the case was retired as diverged
 class MeshInfo(C.Structure):
     _fields_ = [(n, C.c_int) for n in (
         "n_nodes", "n_cells", "n_faces", "n_int_faces", "n_zones",
-        "n_cell_faces", "n_inner", "n_bond1", "n_bond2", "n_tiles")]
+        "n_cell_faces", "n_inner", "n_bond1", "n_bond2", "n_tiles", "n_borrowed", "n_halo",
+        "n_halo_cells", "n_halo_cell_faces")]
 
 
 class MeshArrays(C.Structure):

@@ -23,6 +23,25 @@ def kernel_bytes(info, precision, order, kernel, stage=0, n_borrowed=None):
     z = _sizes(info, precision)
     nC, nF, tot, nT, s = z["nC"], z["nF"], z["tot"], z["nT"], z["s"]
     q = 32  # double4 state
+    if kernel.startswith("k_flux_update") and kernel.endswith(",tg>"):
+        # FP32 float pairs, gradients formed in the tile (no gradient array):
+        # per face info, area vector and the two reconstruction offsets;
+        # per tile face slot the local cell indices, per borrowed slot its
+        # face id; per cell the FP32 state (hi, staged once; halo re-reads
+        # are neighbour re-reads), lo part, 1/V pair, CSR, and per
+        # cell-face the slot, the local neighbour, weights and outward area
+        # vector; per distinct halo cell its cell-faces' neighbour and mode;
+        # the new pair written; Q^n pair read on stage 1
+        nB = getattr(info, "n_borrowed", 0)
+        faces = nF * (4 + 8 + 16) + 4 * (nF + nB) + 4 * nB
+        tiles = 12 * (nT + 1) + 4 * getattr(info, "n_halo", 0)
+        cells = nC * (16 + 16 + 8 + 4 + 32) + tot * (4 + 4 + 8 + 8)
+        cells += 4 * getattr(info, "n_halo_cell_faces", 0)
+        if stage == 1:
+            cells += nC * 32
+        return faces + tiles + cells + nT * 9 * 8
+    if kernel.startswith("k_cfl_dt_pairs"):
+        return nC * (16 + 4 + 8) + tot * 8 + 8 * ((nC + 255) // 256)
     if kernel.startswith("k_flux_update"):
         faces = nF * (8 + 4 + 2 * s + (4 * s if order == 2 else 0))
         tiles = 8 * (nT + 1) + 4 * (n_borrowed or 0)
