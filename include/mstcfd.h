@@ -418,10 +418,14 @@ typedef struct mst_implicit_params {
   /* iterations of the FP32-phase tests (stagnation window, wait for
    * further cases); 0 = 500 */
   int fp32_window;
-  int reserved[1];
+  /* re-freezing (default 500; 0: off): a case whose frozen-limiter L2 has
+   * not fallen below 0.9 of its best for refreeze_window iterations records
+   * the limiter ratios again from its current state (a limiter frozen on
+   * a field still far from the solution can hold a case at a plateau) */
+  int refreeze_window;
 } mst_implicit_params;
 
-/* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-2,
+/* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-1,
  * fp32_until 0, max_iter 20000, graph_iters 20, autotune on,
  * sweep_fp32 off, p_floor 0. */
 void mst_implicit_params_default(mst_implicit_params *p);

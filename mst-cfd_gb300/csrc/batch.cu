@@ -78,6 +78,9 @@ struct mst_batch {
   int* diverged = nullptr;       // per case: retired with a non-finite L2
   int* frozen = nullptr;         // per-case limiter-freezing state
   double* l2_win = nullptr;      // per-case L2 at the last freezing check
+  double* own_first = nullptr;   // per-case L2 of this run's first iteration
+  double* frz_best = nullptr;    // per-case best L2 since its limiter froze
+  int* frz_best_it = nullptr;
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
@@ -236,6 +239,10 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   // the limiter-freezing state machine runs in the FP64 phase only
   na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
   na.l2_win = b->l2_win;
+  na.own_first = b->own_first;
+  na.frz_best = b->frz_best;
+  na.frz_best_it = b->frz_best_it;
+  na.refreeze_window = b->ip.refreeze_window;
   na.freeze_tol = b->ip.freeze_tol;
   na.first_fixed = b->first_fixed ? 1 : 0;
   na.part = b->norm_part;
@@ -347,6 +354,7 @@ void mst_implicit_params_default(mst_implicit_params* p) {
   p->max_iter = 20000;
   p->graph_iters = 20;
   p->autotune = 1;
+  p->refreeze_window = 500;
 }
 
 mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params* cases,
@@ -360,7 +368,8 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
   if (!(ip->cfl0 > 0) || !(ip->cfl_max >= ip->cfl0) || !(ip->omega >= 1.0) || !(ip->tol > 0) ||
       !(ip->freeze_tol >= 0) || !(ip->fp32_until >= 0) ||
       (ip->fp32_until > 0 && p->precision == MST_PREC_FP64_EXACT) ||
-      ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1))
+      ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1) ||
+      ip->refreeze_window < 0)
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
                              "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0, p_floor >= 0 "
@@ -451,6 +460,9 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->iter, sizeof(int))) ||
       (st = balloc(b.get(), &b->frozen, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->l2_win, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->own_first, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->frz_best, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->frz_best_it, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->phi,
                    (size_t)8 * h.n_faces *
                        (p->precision == MST_PREC_FP32 ? sizeof(float) : sizeof(double)))) ||

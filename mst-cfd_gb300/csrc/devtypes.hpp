@@ -187,6 +187,11 @@ struct CaseNormArgs {
   int* iter;               // iteration counter (advanced by k_iter_advance)
   int* frozen;             // [n_cases] limiter-freezing state (or nullptr)
   double* l2_win;          // [n_cases] L2 at the last freezing-window check
+  double* own_first;       // [n_cases] L2 of this run's first iteration (the
+                           // freezing reference, whatever first[] holds)
+  double* frz_best;        // [n_cases] best L2 since the limiter froze
+  int* frz_best_it;        // [n_cases] and its iteration
+  int refreeze_window;     // see mst_implicit_params (0: off)
   double cfl0, cfl_max, tol, freeze_tol;
   int first_fixed;         // first[] holds reference L2s set by the caller
   double* part;            // [n_cases][8] partial sums of (R_rho / V)^2

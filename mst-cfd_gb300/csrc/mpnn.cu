@@ -71,7 +71,7 @@ constexpr int kInK = 64;      // padded K of the first layer
 constexpr int kOut = 4;
 constexpr int kLayers = 3;
 constexpr int kZ = 2 * kW;    // [h, mean of neighbours]
-constexpr int kMaxSplits = 64;  // split-K CTAs of a weight-gradient GEMM
+constexpr int kMaxSplits = 320;  // split-K CTAs of a weight-gradient GEMM
 
 __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -338,7 +338,17 @@ cudaError_t gemm(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, fl
 cudaError_t gemm_wgrad(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, float* C,
                        int M, int N, int K, int ldc) {
   const int kt = K / mst::tc::kBK;  // K tiles
-  const int splits = std::min(kMaxSplits, std::max(1, kt / 8));
+  // about two CTAs per SM over the output tiles, each with at least 4 K tiles
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 148;
+  }
+  const int n_tiles = ((M + mst::tc::kBM - 1) / mst::tc::kBM) * ((N + mst::tc::kBN - 1) / mst::tc::kBN);
+  const int splits =
+      std::min(kMaxSplits, std::max(1, std::min(2 * sms / std::max(1, n_tiles), kt / 4)));
   const int chunk = ((kt + splits - 1) / splits) * mst::tc::kBK;
   const int used = (K + chunk - 1) / chunk;
   mst::tc::GemmArgs g{};

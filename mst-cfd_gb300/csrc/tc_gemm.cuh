@@ -248,10 +248,50 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
     const int row = m0 + warp * 32 + lane;
+    // 16-byte stores where the rows allow them (4 floats of C, 8 BF16 of Cb)
+    const bool vc = !Cout || ((g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(Cout) & 15) == 0);
+    const bool vb = !g.Cb || ((g.ldcb & 7) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 15) == 0);
     for (int c0 = 0; c0 < kBN; c0 += 16) {
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < g.M) {
+      if (row < g.M && vc && vb && n0 + c0 + 16 <= g.N) {
+        const int col0 = n0 + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          float x = v[i];
+          if (!split && g.bias) x += g.bias[col0 + i];
+          if (!split && g.relu) x = fmaxf(x, 0.f);
+          v[i] = x;
+        }
+        if (Cout) {
+          float4* p = reinterpret_cast<float4*>(Cout + (size_t)row * g.ldc + col0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            float4 o = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            if (!split && g.accumulate_c) {
+              const float4 w = p[j];
+              o.x += w.x;
+              o.y += w.y;
+              o.z += w.z;
+              o.w += w.w;
+            }
+            p[j] = o;
+          }
+        }
+        if (g.Cb) {
+          uint4* pb = reinterpret_cast<uint4*>(g.Cb + (size_t)row * g.ldcb + col0);
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            uint32_t w[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * j + 2 * h], v[8 * j + 2 * h + 1]);
+              w[h] = *reinterpret_cast<const uint32_t*>(&b2);
+            }
+            pb[j] = make_uint4(w[0], w[1], w[2], w[3]);
+          }
+        }
+      } else if (row < g.M) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int col = n0 + c0 + i;

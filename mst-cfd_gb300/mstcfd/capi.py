@@ -80,7 +80,7 @@ class ImplicitParams(C.Structure):
                 ("tol", C.c_double), ("freeze_tol", C.c_double), ("fp32_until", C.c_double),
                 ("max_iter", C.c_int), ("graph_iters", C.c_int),
                 ("autotune", C.c_int), ("sweep_fp32", C.c_int), ("p_floor", C.c_double),
-                ("fp32_window", C.c_int), ("reserved", C.c_int * 1)]
+                ("fp32_window", C.c_int), ("refreeze_window", C.c_int)]
 
 
 class BatchInfo(C.Structure):

@@ -112,7 +112,8 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
   double *phi = NULL;
   int frozen = 0; /* 0 live limiter, 1 record this iteration, 2 frozen */
   int converged = 0;
-  double l2_win = 0.0;
+  double l2_win = 0.0, frz_best = 0.0;
+  int frz_best_it = 0;
   if (ip->freeze_tol > 0) {
     phi = (double *)calloc((size_t)8 * (m->n_faces > 0 ? m->n_faces : 1), 8);
     pp.phi = phi;
@@ -140,11 +141,22 @@ int om_lusgs_iterate(const om_mesh *m, const om_params_ext *p, double *q,
      * freeze_tol records the limiter ratios, later ones reuse them */
     if (frozen == 1) {
       frozen = 2;
+      frz_best = l2;
+      frz_best_it = it;
     } else if (phi && frozen == 0 && it > 0 && it % 50 == 0) {
       /* freeze once stagnating below freeze_tol: L2 fell by less than 30%
        * over the last 50 iterations */
       if (first > 0.0 && l2 <= ip->freeze_tol * first && l2 > 0.7 * l2_win) frozen = 1;
       l2_win = l2;
+    } else if (frozen == 2 && ip->refreeze_window > 0) {
+      /* re-freeze: no new best (below 0.9 of it) for refreeze_window
+       * iterations records the ratios again from the current state */
+      if (l2 < 0.9 * frz_best) {
+        frz_best = l2;
+        frz_best_it = it;
+      } else if (it - frz_best_it >= ip->refreeze_window) {
+        frozen = 1;
+      }
     }
     if (ip->tol > 0 && first > 0.0 && l2 <= ip->tol * first) {
       converged = 1; /* the state that met the tolerance is kept */

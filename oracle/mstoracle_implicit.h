@@ -20,6 +20,9 @@ typedef struct om_lusgs_params {
   /* temperature floor: an updated state with p < p_floor * rho gets its
    * internal energy raised to p = p_floor * rho (0: off) */
   double p_floor;
+  /* re-freezing: a frozen case whose L2 has not fallen below 0.9 of its
+   * best for refreeze_window iterations records the ratios again (0: off) */
+  int refreeze_window;
 } om_lusgs_params;
 
 /* niter LU-SGS iterations of one case in place (corrected-mode residual of

@@ -49,7 +49,8 @@ class _OParamsExt(C.Structure):
 
 class _OLusgs(C.Structure):
     _fields_ = [("cfl0", C.c_double), ("cfl_max", C.c_double), ("omega", C.c_double),
-                ("freeze_tol", C.c_double), ("tol", C.c_double), ("p_floor", C.c_double)]
+                ("freeze_tol", C.c_double), ("tol", C.c_double), ("p_floor", C.c_double),
+                ("refreeze_window", C.c_int)]
 
 
 class _ONorms(C.Structure):
@@ -385,12 +386,12 @@ def greedy_colors(mesh):
 
 
 def lusgs_iterate(mesh, prm, q, color, niter, cfl0=5.0, cfl_max=200.0, omega=1.5,
-                  freeze_tol=0.0, tol=0.0, p_floor=0.0):
+                  freeze_tol=0.0, tol=0.0, p_floor=0.0, refreeze_window=500):
     """niter LU-SGS iterations from q; returns (q, L2 history)."""
     q = _f64(q).copy()
     col = np.ascontiguousarray(color, dtype=np.int32)
     ip = _OLusgs(float(cfl0), float(cfl_max), float(omega), float(freeze_tol), float(tol),
-                 float(p_floor))
+                 float(p_floor), int(refreeze_window))
     hist = np.zeros(max(int(niter), 1))
     rc = lib().om_lusgs_iterate(mesh._p, C.byref(prm), _d(q), _i(col), C.byref(ip),
                                 int(niter), _d(hist))

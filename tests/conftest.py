@@ -62,7 +62,8 @@ def golden_cases():
     out = []
     if os.path.isdir(GOLDEN):
         for f in sorted(os.listdir(GOLDEN)):
-            if f.endswith(".npz") and not f.startswith(("lusolver", "writer", "simple")):
+            if f.endswith(".npz") and not f.startswith(("lusolver", "writer", "simple",
+                                                           "shipped")):
                 out.append(os.path.join(GOLDEN, f))
     return out
 

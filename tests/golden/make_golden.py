@@ -27,7 +27,13 @@ the Time loop's residual rows and the Gauss-Seidel iteration counts.
 The GPU tests compare the CUDA path against these arrays bit-for-bit on
 machines where the reference is absent.
 
+shipped.npz: two of the reference's shipped Fluent meshes (2d-stair-un-5-tri,
+triangles; 2d-stair-st-2, quadrilaterals with 20 degenerate NaN-volume cells)
+through the reference's solve() and time loop, outputs stored as SHA-256
+digests (make_shipped).
+
 Run from the repository root:  python tests/golden/make_golden.py
+(only the shipped-mesh fixture:  python tests/golden/make_golden.py shipped)
 """
 import os
 import sys
@@ -200,7 +206,71 @@ def make_simple():
     return path
 
 
+SHIPPED = ("2d-stair-un-5-tri", "2d-stair-st-2")
+
+
+def digest(a):
+    """SHA-256 of an FP64 array's bytes with every NaN made the same quiet
+    NaN (CPU and GPU produce different NaN payloads)."""
+    import hashlib
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    a = np.where(np.isnan(a), np.float64("nan"), a)
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def gentle_state(n, seed):
+    """A state close to rest with small random variations (its 2nd-order
+    reconstruction stays physical); from integer-exact random draws and
+    IEEE arithmetic only, so any machine regenerates it bit for bit."""
+    rng = np.random.default_rng(seed)
+    return mg.primitive_to_q(1.0 + 0.05 * rng.uniform(-1, 1, n), 0.1 * rng.uniform(-1, 1, n),
+                             0.1 * rng.uniform(-1, 1, n), 1.0 + 0.05 * rng.uniform(-1, 1, n))
+
+
+def make_shipped():
+    """Two of the reference's own Fluent meshes (msh/), run through the
+    reference: one solve() for AUSM+ and Roe at 1st order on a random state
+    and at 2nd order on a gentle state (outlets retyped to walls), and five
+    steps of its time loop.  The meshes are stored; the outputs as digests
+    (shipped meshes give large arrays), the initial states as the seeds of
+    generators every machine reproduces exactly."""
+    from oracle import build
+    out = {"meshes": np.array(list(SHIPPED)), "dt": np.array(DT)}
+    for name in SHIPPED:
+        src = os.path.join(build.REF_SRC, "msh", name + ".msh")
+        raw = open(src, "rb").read()
+        out[name + "_msh"] = np.frombuffer(raw, np.uint8)
+        d = tempfile.mkdtemp(prefix="golden_shipped_")
+        msh = os.path.join(d, name + ".msh")
+        with open(msh, "wb") as f:
+            f.write(raw)
+        base = refrun.run(msh, 0, 1, q0=None, dt=DT)
+        nC = len(base.cell_volume)
+        q1 = mg.random_state(nC, seed=11)
+        q2 = gentle_state(nC, seed=12)
+        out[name + "_q0_o1_sha"] = np.array(digest(q1))
+        out[name + "_q0_o2_sha"] = np.array(digest(q2))
+        for flux, fname in ((0, "ausm"), (1, "roe")):
+            for order, q0 in ((1, q1), (2, q2)):
+                r = refrun.run(msh, flux, order, q0=q0, dt=DT, remap5=(order == 2))
+                v = f"{name}_{fname}_o{order}"
+                out[v + "_resid_sha"] = np.array(digest(r.resid))
+                out[v + "_qnew_sha"] = np.array(digest(r.qnew))
+                out[v + "_resid_nan"] = np.array(int(np.isnan(r.resid).any(1).sum()))
+            r = refrun.run(msh, flux, 1, time_steps=5)
+            out[f"{name}_{fname}_steps_q0"] = r.q0
+            out[f"{name}_{fname}_steps_q_sha"] = np.array(digest(r.q_steps))
+            out[f"{name}_{fname}_steps_log"] = r.time_log()
+    path = os.path.join(OUT, "shipped.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["shipped"]:
+        p = make_shipped()
+        print(p, os.path.getsize(p))
+        sys.exit(0)
     for name, mesh in cases():
         p = make(name, mesh)
         print(p, os.path.getsize(p))
