@@ -279,16 +279,21 @@ mst_status launch_flux(mst_ctx* c, const mst::StepArgs& a) {
 
 bool pairs(const mst_ctx* c) { return c->p.precision == MST_PREC_FP32; }
 
-// The FP32 float-pair path at 2nd order in the corrected mode forms its
-// gradients inside the flux kernel (k_flux_update TG: no gradient pass, no
-// gradient through HBM).  MSTCFD_FP32_GRADIENT_PASS=1 in the environment
-// keeps the separate gradient pass instead, to compare the two schedules.
+// The viscous FP32 float-pair path at 2nd order in the corrected mode forms
+// its gradients inside the flux kernel (k_flux_update TG: no gradient pass,
+// no gradient through HBM); measured faster there, while the inviscid stage
+// keeps the gradient pass (its flux kernel alone is issue-bound, and the
+// tile's gradient phases add latency that the pass hides better).  Both
+// schedules give bit-identical states.  MSTCFD_FP32_GRADIENT_PASS=1 / =0 in
+// the environment forces one schedule, to compare them.
 bool tile_grad(const mst_ctx* c) {
-  static const bool pass = [] {
+  static const int force = [] {
     const char* e = std::getenv("MSTCFD_FP32_GRADIENT_PASS");
-    return e && e[0] == '1';
+    return e ? (e[0] == '1' ? 1 : 0) : -1;
   }();
-  return pairs(c) && c->p.order == 2 && c->p.reference_quirks == 0 && !pass;
+  const bool can = pairs(c) && c->p.order == 2 && c->p.reference_quirks == 0;
+  if (force >= 0) return can && force == 0;
+  return can && c->p.viscous;
 }
 
 // double copies of the float-pair states (device order) for the entry
@@ -814,6 +819,8 @@ mst_status mst_ctx_create(const mst_mesh* m, const mst_params* p, mst_ctx** out)
   dm.t_slot_loc = d.t_slot_loc;
   dm.cf_nbl = d.cf_nbl;
   dm.max_halo = L.max_halo;
+  dm.deg3 = 1;
+  for (int i = 0; i <= L.n_cells && dm.deg3; ++i) dm.deg3 = L.c_ptr[i] == 3 * i;
   const size_t nC = L.n_cells, nB = (nC + 255) / 256;
   const size_t qbytes = nC * sizeof(double4_32a);
   if ((st = dalloc(c.get(), &c->q_old, qbytes)) || (st = dalloc(c.get(), &c->q_new, qbytes)) ||

@@ -47,6 +47,7 @@ struct DevMesh {
   const int* t_slot_loc;
   const int* cf_nbl;
   int max_halo;
+  int deg3;  // every cell has three faces and c_ptr[c] = 3c (triangles)
   // batches (nullptr for a single mesh): the case of every device cell and
   // the iteration at which each case converged (-1 while it runs).  The
   // residual kernels skip the cells of converged cases: after the
@@ -54,6 +55,13 @@ struct DevMesh {
   const int* c_case;
   const int* case_conv;
 };
+
+// the cell-face range of device cell c: [3c, 3c + 3) without a load on
+// meshes of triangles only
+__device__ __forceinline__ int2 cell_face_range(const DevMesh& m, int c) {
+  if (m.deg3) return make_int2(3 * c, 3 * c + 3);
+  return make_int2(m.c_ptr[c], m.c_ptr[c + 1]);
+}
 
 // true when device cell c belongs to a converged case of a batch
 __device__ __forceinline__ bool cell_case_done(const DevMesh& m, int c) {
