@@ -15,19 +15,25 @@ Arms:
                      residual sums as unevaluated FP32 pairs, no FP64
                      instruction) with the state resident
                      in HBM, timed with CUDA events on the context's stream;
-                     "fp64" = the same in FP64; "e2e" = FP32 through the
-                     public API with the state copied host->device and back
-                     every step from page-locked host buffers.
+                     "fp64" = the same in FP64 (with its FP64-pipe
+                     roofline); "e2e" = FP32 through the public API with
+                     host buffers: each step a job of mst_step_host_jobs,
+                     its state copied host->device and back (page-locked
+                     buffers), the copies overlapped with the neighbouring
+                     jobs' computation.
   --impl reference   the CPU restatement of the same path (the oracle,
                      OpenMP over all host cores) on the same workload.
 
 The line also carries "batch": the batched steady-wedge family (the
 compression-ramp cases of mstcfd.meshgen.wedge_family: seeded Mach U[1.5,3],
-ramp angle U[5,15] deg redrawn within 1 deg of shock detachment, Re
-U[1e3,1e4], laminar, Roe + minmod) solved from
-free stream (cold start) to L2 1e-8 by the batched LU-SGS path in FP64 --
-wall time of the whole batch, iterations, cases converged; --batch-cases
-and --batch-cells set its size (0 cases: skipped).
+ramp angle U[5,15] deg redrawn while the inviscid post-shock Mach is below
+1.2, Re U[1e3,1e4], laminar, Roe + minmod) solved from free stream (cold
+start) to L2 1e-8 by the batched LU-SGS path in FP64 and with the
+production options -- wall time of the whole batch, iterations, cases
+converged -- and from the learned initial field with the same options
+(batch.warm); --batch-cases and --batch-cells set its size (0 cases:
+skipped); "tgv3d" the 3D Taylor-Green vortex; "simple" the pressure-based
+SIMPLE solver.
 
 One JSON line on rank 0.  Under torchrun each rank runs an independent
 replica on its own GPU (single-mesh runs do not shard: replicas only).
@@ -375,11 +381,28 @@ def run_gpu(args, ws, rank, local, grp):
                          avg_launch_ms=round(avg_ms, 5), kernel_share=share), nC
 
 
+def _ramp_mesh(p):
+    from mstcfd import meshgen as mg
+    return mg.wedge(p["cells"], p["angle"], seed=p["seed"])
+
+
+def _ramp_meshes(fam):
+    """The ramp meshes of a family, generated on the host's cores (fresh
+    interpreters: nothing of this process's CUDA state is inherited)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    workers = min(16, os.cpu_count() or 1, len(fam))
+    if workers <= 1:
+        return [_ramp_mesh(p) for p in fam]
+    with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_ramp_mesh, fam, chunksize=4))
+
+
 def _wedge_cases(n_cases, lo, hi):
     """Seeded compression-ramp family: (mesh dict, Mach, angle, Re)."""
     from mstcfd import meshgen as mg
-    return [(mg.wedge(p["cells"], p["angle"], seed=p["seed"]), p["mach"], p["angle"],
-             p["reynolds"]) for p in mg.wedge_family(n_cases, cells=(lo, hi))]
+    fam = mg.wedge_family(n_cases, cells=(lo, hi))
+    return [(m, p["mach"], p["angle"], p["reynolds"]) for m, p in zip(_ramp_meshes(fam), fam)]
 
 
 # temperature floor of the batched LU-SGS solves, p >= P_FLOOR rho (1.4% of
@@ -497,8 +520,11 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
     from mstcfd.mpnn import Network
     t0 = time.perf_counter()
     train = []
-    for p in mg.wedge_family(args.warm_train, cells=(4000, 12000), seed=777):
-        m, cp = ws.case_setup(p)
+    # ramps of the batch's own size range (a network trained on coarser
+    # ramps of 4k-12k cells gained nothing on these), seeds disjoint
+    tfam = mg.wedge_family(args.warm_train, cells=tuple(args.batch_cells), seed=777)
+    for p, m in zip(tfam, _ramp_meshes(tfam)):
+        cp = ws.case_params_of(p)
         mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
                                 m["n_cells"])
         train.append((p, m, mesh, cp))
@@ -579,7 +605,8 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
             "speedup_same_options": {"fp64": warm64["speedup_vs_cold_same_options"],
                                      "production": warm_m["speedup_vs_cold_same_options"]},
             "warm_production_vs_plain_fp64_cold": round(wall_cold / warm_m["value"], 3),
-            "train": {"cases": args.warm_train, "converged": len(samples), "cells": "4000-12000",
+            "train": {"cases": args.warm_train, "converged": len(samples),
+                      "cells": f"{args.batch_cells[0]}-{args.batch_cells[1]}",
                       "seeds": "disjoint from the batch", "steps": args.warm_steps,
                       "loss_first": round(float(hist[0]), 5),
                       "loss_last": round(float(hist[-20:].mean()), 5),
@@ -587,6 +614,24 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
                                      for i in range(0, len(hist), max(1, len(hist) // 8))],
                       "data_s": round(data_s, 2), "train_s": round(train_s, 2)},
             "network_gemm": gemm}
+
+
+def run_network_only(args):
+    """Network GEMMs over the batch's cases (features of the ramp family)."""
+    from mstcfd import Mesh, warmstart as ws
+    from mstcfd.mpnn import Network
+    fam = _wedge_cases(args.batch_cases, args.batch_cells[0], args.batch_cells[1])
+    feats = []
+    for m, mach, angle, re in fam:
+        mesh = Mesh.from_arrays(m["node_xy"], m["face_nodes"], m["face_cells"], m["zones"],
+                                m["n_cells"])
+        ptr, nbr = ws.neighbours(m)
+        feats.append((ws.features(m, mesh.arrays(), dict(mach=mach, angle=angle, reynolds=re)),
+                      ptr, nbr, mach))
+    net = Network(seed=11)
+    out = _gemm_at_scale(net, feats)
+    net.close()
+    return out
 
 
 def run_cpu_sample(m, steps, budget_s=30.0):
@@ -836,9 +881,9 @@ def main():
                     help="cases of the batched wedge solve (0: skip)")
     ap.add_argument("--batch-cells", type=int, nargs=2, default=[20000, 60000])
     ap.add_argument("--batch-iters", type=int, default=20000)
-    ap.add_argument("--warm-train", type=int, default=128,
+    ap.add_argument("--warm-train", type=int, default=256,
                     help="training cases of the learned warm start (0: no warm start)")
-    ap.add_argument("--warm-steps", type=int, default=800)
+    ap.add_argument("--warm-steps", type=int, default=2000)
     ap.add_argument("--fp32-until", type=float, default=1e-5,
                     help="the batch's production runs use the FP32 residual until this L2")
     ap.add_argument("--fp32-window", type=int, default=1000,
@@ -850,6 +895,8 @@ def main():
     ap.add_argument("--tgv-n", type=int, default=128,
                     help="hexahedra per side of the 3D Taylor-Green mesh (x6 cells; 0: skip)")
     ap.add_argument("--tgv-steps", type=int, default=10)
+    ap.add_argument("--network-only", action="store_true",
+                    help="time only the network's GEMMs at batch scale (profiling)")
     ap.add_argument("--no-simple", action="store_true",
                     help="skip the pressure-based SIMPLE sub-line")
     args = ap.parse_args()
@@ -885,6 +932,11 @@ def main():
         print(json.dumps(line))
         return
     grp = _Group(ws)
+    if args.network_only:
+        # the learned initial field's tensor-core GEMMs alone, at batch scale
+        # (one forward + backward over the batch's cells, untrained weights)
+        print(json.dumps({"network_gemm": run_network_only(args)}))
+        return
     results, roof, nC = run_gpu(args, ws, rank, local, grp)
     batch_line = run_batch(args, ws, rank, grp) if args.batch_cases > 0 else None
     tgv_line = run_tgv3d(args, grp) if args.tgv_n > 0 else None

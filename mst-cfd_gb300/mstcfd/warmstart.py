@@ -25,14 +25,18 @@ GAMMA = 1.4
 CV = 1.0 / (GAMMA * (GAMMA - 1.0))
 
 
+def case_params_of(p):
+    """Batch case parameters of one family member (free stream, laminar
+    transport coefficients of its Reynolds number)."""
+    from . import batch
+    mu = p["mach"] / p["reynolds"]
+    return batch.case_params(mg.freestream(p["mach"]), mu=mu, lambda_=-2.0 / 3.0 * mu,
+                             kappa=mu * GAMMA * CV / 0.72, cv=CV)
+
+
 def case_setup(p):
     """Mesh dict and batch case parameters of one family member."""
-    from . import batch
-    m = mg.wedge(p["cells"], p["angle"], seed=p["seed"])
-    mu = p["mach"] / p["reynolds"]
-    cp = batch.case_params(mg.freestream(p["mach"]), mu=mu, lambda_=-2.0 / 3.0 * mu,
-                           kappa=mu * GAMMA * CV / 0.72, cv=CV)
-    return m, cp
+    return mg.wedge(p["cells"], p["angle"], seed=p["seed"]), case_params_of(p)
 
 
 def neighbours(m):
