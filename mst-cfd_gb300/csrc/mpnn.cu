@@ -25,8 +25,10 @@ constexpr uint32_t kLBO = 128, kSBO = 1024;
 std::atomic<long long> g_wait_limit{-1};
 
 cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
-  static std::atomic<uint64_t> attr_done{0};
-  cudaError_t e = ensure_smem_limit(k_gemm_bf16, kSmemBytes, attr_done);
+  static std::atomic<uint64_t> attr_done{0}, attr_done16{0};
+  const bool narrow = a0.N <= 16;
+  cudaError_t e = narrow ? ensure_smem_limit(k_gemm_bf16<16>, smem_bytes<16>(), attr_done16)
+                         : ensure_smem_limit(k_gemm_bf16<kBN>, kSmemBytes, attr_done);
   if (e != cudaSuccess) return e;
   GemmArgs a = a0;
   const long long lim = g_wait_limit.load(std::memory_order_relaxed);
@@ -36,8 +38,13 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
     a.sbo = kSBO;
   }
   const int splits = a.k_chunk > 0 ? (a.K + a.k_chunk - 1) / a.k_chunk : 1;
+  if (narrow) {
+    dim3 grid((a.M + kBM - 1) / kBM, 1, splits);
+    k_gemm_bf16<16><<<grid, 128, smem_bytes<16>(), s>>>(a);
+    return cudaGetLastError();
+  }
   dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN, splits);
-  k_gemm_bf16<<<grid, 128, kSmemBytes, s>>>(a);
+  k_gemm_bf16<kBN><<<grid, 128, kSmemBytes, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -161,19 +168,32 @@ __global__ void k_agg_back(const float* __restrict__ dhn, const float* __restric
   dh[(size_t)j * kW + k] = v;
 }
 
-// column sums of g[n][w] into out[w] (bias gradients), fixed order
-__global__ void k_colsum(const float* __restrict__ g, int n, int w, float* __restrict__ out) {
+// Column sums of g[n][w] (bias gradients), w dividing 256, in a fixed order
+// (deterministic): block b sums rows [b*chunk, (b+1)*chunk), its 256 threads
+// reading whole rows (thread t: column t % w, row offset t / w), into
+// part[b][w]; k_colsum_parts then adds the blocks' partials in block order.
+__global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ g, int n, int w,
+                                                int chunk, float* __restrict__ part) {
   __shared__ float red[256];
-  const int col = blockIdx.x;
+  const int t = threadIdx.x, col = t % w, rows = 256 / w;
+  const int r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
   float s = 0.f;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) s += g[(size_t)r * w + col];
-  red[threadIdx.x] = s;
+  for (int r = r0 + t / w; r < r1; r += rows) s += g[(size_t)r * w + col];
+  red[t] = s;
   __syncthreads();
-  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-    __syncthreads();
+  if (t < w) {
+    float acc = red[t];
+    for (int k = 1; k < rows; ++k) acc += red[t + k * w];
+    part[(size_t)blockIdx.x * w + t] = acc;
   }
-  if (threadIdx.x == 0) out[col] = red[0];
+}
+__global__ void k_colsum_parts(const float* __restrict__ part, int blocks, int w,
+                               float* __restrict__ out) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= w) return;
+  float acc = 0.f;
+  for (int b = 0; b < blocks; ++b) acc += part[(size_t)b * w + col];
+  out[col] = acc;
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
@@ -373,6 +393,15 @@ cudaError_t gemm_wgrad(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16*
   return cudaGetLastError();
 }
 
+// bias gradient out[w] = column sums of g[n][w], through the split-K
+// partial buffer (free between weight-gradient GEMMs)
+void colsum(mst_mpnn* m, const float* g, int n, int w, float* out) {
+  const int blocks = std::max(1, std::min(296, (n + 255) / 256));
+  const int chunk = (n + blocks - 1) / blocks;
+  k_colsum<<<blocks, 256>>>(g, n, w, chunk, m->part);
+  k_colsum_parts<<<(w + 127) / 128, 128>>>(m->part, blocks, w, out);
+}
+
 cudaError_t transpose(const __nv_bfloat16* src, int n, int w, int n_pad, __nv_bfloat16* dst) {
   dim3 grid((n_pad + 31) / 32, (w + 31) / 32), block(32, 8);
   k_transpose_bf16<<<grid, block>>>(src, n, w, n_pad, dst);
@@ -429,7 +458,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
   if (e == cudaSuccess)
     e = gemm_wgrad(m, m->tA, m->tB, P(m, kWd).g, kOut, kW, nk, kW);
   if (e != cudaSuccess) return e;
-  k_colsum<<<kOut, 256>>>(m->dY, n, kOut, P(m, kBd).g);
+  colsum(m, m->dY, n, kOut, P(m, kBd).g);
   // dH3 = dY . Wd : B operand = Wd^T [128][64] (K = 4 padded with zeros)
   e = transpose(P(m, kWd).wb, kOut, kW, kInK, m->WdT);
   if (e == cudaSuccess) e = gemm(m, m->dYb, m->WdT, m->dH, np, kW, kInK, kW, nullptr, 0, 0);
@@ -443,7 +472,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
     if (e == cudaSuccess)
       e = gemm_wgrad(m, m->tA, m->tB, P(m, wl(l)).g, kW, kZ, nk, kZ);
     if (e != cudaSuccess) break;
-    k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, bl(l)).g);
+    colsum(m, m->dP, n, kW, P(m, bl(l)).g);
     // dZ = dP . Wl : B operand = Wl^T [256][128]
     e = transpose(P(m, wl(l)).wb, kW, kZ, kW, m->WlT);
     if (e == cudaSuccess) e = gemm(m, m->dPb, m->WlT, m->dZ, np, kZ, kW, kZ, nullptr, 0, 0);
@@ -462,7 +491,7 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
     if (e == cudaSuccess) e = transpose(m->X, n, kInK, nk, m->tB);
     if (e == cudaSuccess)
       e = gemm_wgrad(m, m->tA, m->tB, P(m, kWe).g, kW, kInK, nk, kInK);
-    if (e == cudaSuccess) k_colsum<<<kW, 256>>>(m->dP, n, kW, P(m, kBe).g);
+    if (e == cudaSuccess) colsum(m, m->dP, n, kW, P(m, kBe).g);
   }
   return e == cudaSuccess ? cudaGetLastError() : e;
 }

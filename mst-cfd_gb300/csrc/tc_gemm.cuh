@@ -6,7 +6,7 @@
 //   C[M, N] (FP32) = A[M, K] (BF16, row-major) . B[N, K]^T (BF16, row-major)
 //                    (+ bias[N]) (ReLU) ; optional BF16 copy of C
 //
-// One CTA of 128 threads per 128 x BN tile (BN = 128).  K is walked in
+// One CTA of 128 threads per 128 x BN tile (BN = 128, or 16 when N <= 16).  K is walked in
 // 64-wide tiles through two shared-memory stages filled with cp.async in
 // the canonical no-swizzle K-major layout of the MMA descriptors (8 x 16-
 // byte core matrices; core matrices adjacent in K 128 bytes apart, 8-row
@@ -27,9 +27,17 @@ namespace tc {
 
 constexpr int kBM = 128, kBN = 128, kBK = 64;
 constexpr int kTileA = kBM * kBK * 2;  // bytes
-constexpr int kTileB = kBN * kBK * 2;
 constexpr int kStages = 2;
-constexpr int kSmemBytes = kStages * (kTileA + kTileB) + 64;
+// output tile width BN: 128, or 16 for narrow outputs (N <= 16; the MMA
+// instruction's smallest N at M = 128)
+template <int BN>
+__host__ __device__ constexpr int tile_b_bytes() { return BN * kBK * 2; }
+template <int BN>
+__host__ __device__ constexpr int smem_bytes() { return kStages * (kTileA + tile_b_bytes<BN>()) + 64; }
+constexpr int kSmemBytes = smem_bytes<kBN>();
+// tensor-memory columns allocated for a BN-wide accumulator (a power of two >= 32)
+template <int BN>
+__host__ __device__ constexpr int tmem_cols() { return BN < 32 ? 32 : BN; }
 constexpr unsigned kSpinLimit = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -138,7 +146,10 @@ struct GemmArgs {
   int k_chunk;
 };
 
+template <int BN = kBN>
 __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
+  constexpr int kTileB = tile_b_bytes<BN>();
+  constexpr int kBN = BN;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;
   uint8_t* sB = smem + kStages * kTileA;
@@ -156,7 +167,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tslot)),
-                 "r"(kBN));
+                 "r"(tmem_cols<BN>()));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
@@ -312,7 +323,8 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(tmem_cols<BN>()));
 }
 
 }  // namespace tc
