@@ -40,11 +40,11 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   const int splits = a.k_chunk > 0 ? (a.K + a.k_chunk - 1) / a.k_chunk : 1;
   if (narrow) {
     dim3 grid((a.M + kBM - 1) / kBM, 1, splits);
-    k_gemm_bf16<16><<<grid, 128, smem_bytes<16>(), s>>>(a);
+    k_gemm_bf16<16><<<grid, kGemmThreads, smem_bytes<16>(), s>>>(a);
     return cudaGetLastError();
   }
   dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN, splits);
-  k_gemm_bf16<kBN><<<grid, 128, kSmemBytes, s>>>(a);
+  k_gemm_bf16<kBN><<<grid, kGemmThreads, kSmemBytes, s>>>(a);
   return cudaGetLastError();
 }
 
