@@ -479,6 +479,11 @@ def run_batch(args, ws, rank, grp):
            "iterations": r["iterations"], "max_iter": args.batch_iters,
            "median_case_iterations": int(np.median(conv[conv >= 0])) if (conv >= 0).any() else None,
            "Mcell_iterations_per_s": round(cells * r["iterations"] / (r["ms"] * 1e-3) / 1e6, 1),
+           # the work actually done: each case's cells times the iterations
+           # it ran (a converged case costs nothing afterwards)
+           "case_Mcell_iterations_per_s": round(
+               sum(m.n_cells * (int(c) + 1 if c >= 0 else r["iterations"])
+                   for (m, _), c in zip(cases, conv)) / (r["ms"] * 1e-3) / 1e6, 1),
            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
            "graph_iters": info["graph_iters"],
            "workload": (f"{len(cases)} compression ramps (no-slip flat plate and ramp), "
