@@ -7,11 +7,13 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "ctx.hpp"
 #include "tc_gemm.cuh"
+#include "tc_gemm_tma.cuh"
 
 namespace mst {
 namespace tc {
@@ -24,6 +26,75 @@ constexpr uint32_t kLBO = 128, kSBO = 1024;
 // polls of the GEMM's bounded mbarrier waits (mst_set_wait_limit)
 std::atomic<long long> g_wait_limit{-1};
 
+// cuTensorMapEncodeTiled, through the runtime's driver entry point (no
+// link-time dependency on the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// tensor map of a row-major [rows][K] BF16 matrix in 128-row x 64-K boxes,
+// 128-byte swizzle; rows beyond the matrix read as zeros
+bool bf16_tile_map(CUtensorMap* map, const void* base, int rows, int K) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+            box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+// The persistent TMA kernel where it applies (whole K per CTA, K <= 256 in
+// tiles of 64, at least 17 outputs, 16-byte-aligned operands); false: the
+// caller launches k_gemm_bf16 instead
+bool gemm_tma(const GemmArgs& a, cudaStream_t s, cudaError_t* err) {
+  *err = cudaSuccess;
+  if (a.k_chunk > 0 || a.N <= 16 || a.K % kBK != 0 || a.K / kBK > kTmaMaxKT || a.M <= 0 ||
+      (reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.B) & 15))
+    return false;
+  CUtensorMap ma, mb;
+  if (!bf16_tile_map(&ma, a.A, a.M, a.K) || !bf16_tile_map(&mb, a.B, a.N, a.K)) return false;
+  static std::atomic<uint64_t> attr_done{0};
+  const int kt = a.K / kBK;
+  *err = ensure_smem_limit(k_gemm_tma, tma_smem_bytes(kTmaMaxKT), attr_done);
+  if (*err != cudaSuccess) return true;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 148;
+  }
+  TmaGemm t;
+  t.g = a;
+  t.kt = kt;
+  t.n_ntiles = (a.N + kBN - 1) / kBN;
+  t.m_tiles = (a.M + kBM - 1) / kBM;
+  // two resident CTAs per SM, each column block with the same number of CTAs
+  int grid = std::min(2 * sms, t.n_ntiles * t.m_tiles);
+  grid = std::max(t.n_ntiles, grid / t.n_ntiles * t.n_ntiles);
+  k_gemm_tma<<<grid, kTmaThreads, tma_smem_bytes(kt), s>>>(ma, mb, t);
+  *err = cudaGetLastError();
+  return true;
+}
+
 cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   static std::atomic<uint64_t> attr_done{0}, attr_done16{0};
   const bool narrow = a0.N <= 16;
@@ -34,6 +105,8 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   const long long lim = g_wait_limit.load(std::memory_order_relaxed);
   a.spin_limit = lim < 0 ? kSpinLimit : (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
   if (a.lbo == 0) {
+    cudaError_t te;
+    if (gemm_tma(a, s, &te)) return te;
     a.lbo = kLBO;
     a.sbo = kSBO;
   }
@@ -662,6 +735,8 @@ mst_status mst_mpnn_forward(mst_mpnn* m, float* y) {
   if (e == cudaSuccess && y)
     e = cudaMemcpy(y, m->Y, sizeof(float) * (size_t)m->n * kOut, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn forward: ") + cudaGetErrorString(e));
+  if (herr == 2)
+    return mst_internal_fail(MST_ECUDA, "mpnn forward: shared memory not 1024-byte aligned for TMA");
   if (herr) return mst_internal_fail(MST_ETIMEOUT, "mpnn forward: a tensor-core wait timed out");
   return MST_OK;
 }
@@ -673,6 +748,8 @@ mst_status mst_mpnn_backward(mst_mpnn* m, double* loss) {
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("mpnn backward: ") + cudaGetErrorString(e));
+  if (herr == 2)
+    return mst_internal_fail(MST_ECUDA, "mpnn backward: shared memory not 1024-byte aligned for TMA");
   if (herr) return mst_internal_fail(MST_ETIMEOUT, "mpnn backward: a tensor-core wait timed out");
   if (loss) *loss = l;
   return MST_OK;
@@ -791,6 +868,8 @@ mst_status mst_tc_gemm_check(const uint16_t* A, const uint16_t* B, const float* 
   if (e == cudaSuccess) e = cudaMemcpy(C, dC, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost);
   cleanup();
   if (e != cudaSuccess) return mst_internal_fail(MST_ECUDA, std::string("gemm: ") + cudaGetErrorString(e));
+  if (herr == 2)
+    return mst_internal_fail(MST_ECUDA, "gemm: shared memory not 1024-byte aligned for TMA");
   if (herr) return mst_internal_fail(MST_ETIMEOUT, "gemm: a tensor-core wait timed out");
   return MST_OK;
 }

@@ -146,6 +146,66 @@ struct GemmArgs {
   int k_chunk;
 };
 
+// Epilogue of 16 accumulator columns of one row: bias, ReLU, the residual
+// add (accumulate_c) and the stores of C and its BF16 copy (16-byte stores
+// where the row allows them; vc / vb: C / Cb rows 16-byte aligned).
+__device__ __forceinline__ void store16(const GemmArgs& g, bool split, float* Cout, int row,
+                                        int n0, int c0, float v[16], bool vc, bool vb) {
+  if (row < g.M && vc && vb && n0 + c0 + 16 <= g.N) {
+    const int col0 = n0 + c0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      float x = v[i];
+      if (!split && g.bias) x += g.bias[col0 + i];
+      if (!split && g.relu) x = fmaxf(x, 0.f);
+      v[i] = x;
+    }
+    if (Cout) {
+      float4* p = reinterpret_cast<float4*>(Cout + (size_t)row * g.ldc + col0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float4 o = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        if (!split && g.accumulate_c) {
+          const float4 w = p[j];
+          o.x += w.x;
+          o.y += w.y;
+          o.z += w.z;
+          o.w += w.w;
+        }
+        p[j] = o;
+      }
+    }
+    if (g.Cb) {
+      uint4* pb = reinterpret_cast<uint4*>(g.Cb + (size_t)row * g.ldcb + col0);
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        uint32_t w[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * j + 2 * h], v[8 * j + 2 * h + 1]);
+          w[h] = *reinterpret_cast<const uint32_t*>(&b2);
+        }
+        pb[j] = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+  } else if (row < g.M) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int col = n0 + c0 + i;
+      float x = v[i];
+      if (!split && g.bias && col < g.N) x += g.bias[col];
+      if (!split && g.relu) x = fmaxf(x, 0.f);
+      if (col < g.N) {
+        if (Cout) {
+          float* p = Cout + (size_t)row * g.ldc + col;
+          *p = (!split && g.accumulate_c) ? *p + x : x;
+        }
+        if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
+      }
+    }
+  }
+}
+
 // threads of a CTA; in the epilogue warp w reads TMEM lanes 32 w.. (its
 // rows).  (256 threads, with the columns split over two warp groups, measured
 // slower: 5.6 against 4.0 ms for the network's 14 GEMMs at batch scale.)
@@ -270,59 +330,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_bf16(const GemmArgs g) {
     for (int c0 = 0; c0 < kBN; c0 += 16) {
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < g.M && vc && vb && n0 + c0 + 16 <= g.N) {
-        const int col0 = n0 + c0;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          float x = v[i];
-          if (!split && g.bias) x += g.bias[col0 + i];
-          if (!split && g.relu) x = fmaxf(x, 0.f);
-          v[i] = x;
-        }
-        if (Cout) {
-          float4* p = reinterpret_cast<float4*>(Cout + (size_t)row * g.ldc + col0);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            float4 o = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            if (!split && g.accumulate_c) {
-              const float4 w = p[j];
-              o.x += w.x;
-              o.y += w.y;
-              o.z += w.z;
-              o.w += w.w;
-            }
-            p[j] = o;
-          }
-        }
-        if (g.Cb) {
-          uint4* pb = reinterpret_cast<uint4*>(g.Cb + (size_t)row * g.ldcb + col0);
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            uint32_t w[4];
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-              const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * j + 2 * h], v[8 * j + 2 * h + 1]);
-              w[h] = *reinterpret_cast<const uint32_t*>(&b2);
-            }
-            pb[j] = make_uint4(w[0], w[1], w[2], w[3]);
-          }
-        }
-      } else if (row < g.M) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int col = n0 + c0 + i;
-          float x = v[i];
-          if (!split && g.bias && col < g.N) x += g.bias[col];
-          if (!split && g.relu) x = fmaxf(x, 0.f);
-          if (col < g.N) {
-            if (Cout) {
-              float* p = Cout + (size_t)row * g.ldc + col;
-              *p = (!split && g.accumulate_c) ? *p + x : x;
-            }
-            if (g.Cb) g.Cb[(size_t)row * g.ldcb + col] = __float2bfloat16_rn(x);
-          }
-        }
-      }
+      store16(g, split, Cout, row, n0, c0, v, vc, vb);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
