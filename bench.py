@@ -419,8 +419,9 @@ def _production(args):
 
 
 def _production_label(args):
-    return (f"FP32 residual until L2 {args.fp32_until:g} (window {args.fp32_window}), then "
-            f"FP64; FP32 sweeps, FP64 diagonal inversion and update")
+    return (f"FP32 residual until each case's L2 is {args.fp32_until:g} of its first (or "
+            f"stagnates for {args.fp32_window} iterations), then FP64, case by case; FP32 "
+            f"sweeps, FP64 diagonal inversion and update")
 
 
 def _batch_solve(cases, q0, imp, grp, l2_ref=None):
@@ -486,6 +487,10 @@ def run_batch(args, ws, rank, grp):
                    for (m, _), c in zip(cases, conv)) / (r["ms"] * 1e-3) / 1e6, 1),
            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
            "graph_iters": info["graph_iters"],
+           # the cases left at the cap (at most 16): cells and L2 / first L2
+           "not_converged": [{"cells": int(m.n_cells),
+                              "l2_ratio": float(st["last_l2"][i] / st["first_l2"][i])}
+                             for i, (m, _) in enumerate(cases) if conv[i] < 0][:16],
            "workload": (f"{len(cases)} compression ramps (no-slip flat plate and ramp), "
                         f"{args.batch_cells[0]}-"
                         f"{args.batch_cells[1]} triangles each, Mach U[1.5,3], angle U[5,15] deg "
@@ -503,6 +508,10 @@ def run_batch(args, ws, rank, grp):
                          "iterations": rm["iterations"],
                          "median_case_iterations": int(np.median(cm[cm >= 0]))
                          if (cm >= 0).any() else None,
+                         "not_converged": [{"cells": int(m.n_cells),
+                                            "l2_ratio": float(stm["last_l2"][i]
+                                                              / stm["first_l2"][i])}
+                                           for i, (m, _) in enumerate(cases) if cm[i] < 0][:16],
                          "precision": _production_label(args)}
     if args.warm_train > 0:
         out["warm"] = run_warm(args, fam, cases, q0, q_cold, conv, first_cold, cm, wall,

@@ -393,13 +393,14 @@ typedef struct mst_implicit_params {
    * dropped) until density and pressure stay above a fifth of their
    * current values. */
   double freeze_tol;
-  /* mixed precision (FP64 production path only): a solve starts with the
-   * FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps and
-   * state) and switches to the FP64 residual once every unconverged case
-   * is below fp32_until * L2_first or stagnating in FP32 (its L2 has not
-   * fallen by 10% for fp32_window iterations: the FP32 residual's floor),
-   * or once at least half are and no further case has joined them for
-   * fp32_window iterations; 0: FP64 residual throughout */
+  /* mixed precision (FP64 production path only): every case starts with
+   * the FP32 residual (FP32 gradient, reconstruction and flux; FP64 sweeps
+   * and state) and switches, on its own, to the FP64 residual once it is
+   * below fp32_until * L2_first or stagnating in FP32 (its L2 has not
+   * fallen by 10% for fp32_window iterations: the FP32 residual's floor);
+   * cases in the two phases iterate side by side (one residual pass per
+   * phase, each skipping the other phase's cases); 0: FP64 residual
+   * throughout */
   double fp32_until;
   int max_iter;     /* iteration limit of mst_batch_solve */
   int graph_iters;  /* iterations per CUDA-graph launch (even; 0: no graph) */
@@ -415,8 +416,7 @@ typedef struct mst_implicit_params {
    * momentum kept).  Without it a near-vacuum cell at a slip / no-slip
    * corner rejects every update (positivity) and freezes its case. */
   double p_floor;
-  /* iterations of the FP32-phase tests (stagnation window, wait for
-   * further cases); 0 = 500 */
+  /* iterations of the FP32-phase stagnation test; 0 = 500 */
   int fp32_window;
   /* re-freezing (default 500; 0: off): a case whose frozen-limiter L2 has
    * not fallen below 0.9 of its best for refreeze_window iterations records

@@ -89,14 +89,16 @@ struct mst_batch {
   bool first_fixed = false;      // reference L2s set by mst_batch_set_l2_ref
   double* norm_part = nullptr;   // [n_cases][8] partial L2 sums
   int cur = 0;                   // which of ctx->q_old / q_new holds Q
-  // mixed precision: FP32 residual (FP32 state copy, FP32 gradient) while
-  // lo is set, FP64 afterwards; the sweeps are FP64 throughout
+  // mixed precision: each case evaluates the FP32 residual (FP32 state
+  // copy, FP32 gradient) until it is ready for the FP64 one; lo is set
+  // while any case is still in the FP32 phase (case_lo / lo_h: per case)
   bool lo = false;
   void* grad32 = nullptr;
+  int* case_lo = nullptr;
+  std::vector<int> lo_h;
   // phase-switch bookkeeping: per case the best FP32-phase L2 and when
   std::vector<double> lo_best;
   std::vector<int> lo_best_it;
-  int lo_ready_max = 0, lo_ready_since = 0;
   bool tuned = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [FP64 phase, FP32 phase]
   int graph_iters[2] = {0, 0};
@@ -130,21 +132,22 @@ float4* qfbuf(mst_batch* b, int which) {
 
 bool exact(const mst_batch* b) { return b->ctx->p.precision == MST_PREC_FP64_EXACT; }
 
-// the residual R(Q) of the current state into ctx->r
-mst_status enqueue_residual(mst_batch* b, int which) {
+// the residual R(Q) of the current state into ctx->r for the cases that
+// dm admits, in the FP32 (lo) or the solve's own precision
+mst_status residual_pass(mst_batch* b, int which, bool lo, const mst::DevMesh& dm) {
   mst_ctx* c = b->ctx;
-  const int prec = b->lo ? MST_PREC_FP32 : c->p.precision;
-  void* grad = b->lo ? b->grad32 : c->grad;
+  const int prec = lo ? MST_PREC_FP32 : c->p.precision;
+  void* grad = lo ? b->grad32 : c->grad;
   cudaStream_t s = c->stream;
   const double4_32a* q = qbuf(b, which);
   const float4* qf = qfbuf(b, which);
   cudaError_t e = cudaSuccess;
   if (c->p.order == 2) {
-    if (exact(b) && !b->lo) e = mst::exact::launch_gradient(prec, c->dm, q, grad, 0, s);
+    if (exact(b) && !lo) e = mst::exact::launch_gradient(prec, dm, q, grad, 0, s);
     else if (qf)
-      e = mst::fast::launch_gradient_dt(prec, c->dm, q, qf, grad, 0, 0.0, nullptr, nullptr,
+      e = mst::fast::launch_gradient_dt(prec, dm, q, qf, grad, 0, 0.0, nullptr, nullptr,
                                         nullptr, s);
-    else e = mst::fast::launch_gradient(prec, c->dm, q, grad, 0, s);
+    else e = mst::fast::launch_gradient(prec, dm, q, grad, 0, s);
     if (e != cudaSuccess)
       return mst_internal_fail(MST_ECUDA, std::string("gradient: ") + cudaGetErrorString(e));
   }
@@ -158,16 +161,30 @@ mst_status enqueue_residual(mst_batch* b, int which) {
   mst::set_physics(a, c->p.inlet_q, c->p.viscous, c->p.mu, c->p.lambda, c->p.kappa, c->p.cv);
   a.case_tab = b->case_tab;
   a.case_tab_f = b->case_tab_f;
-  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE && !b->lo) {
+  if (b->ip.freeze_tol > 0 && c->p.order == 2 && c->p.limiter != MST_LIMITER_NONE && !lo) {
     a.case_frozen = b->frozen;
     a.phi = b->phi;
   }
-  e = (exact(b) && !b->lo)
-          ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s)
-          : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, c->dm, a, 0, s);
+  e = (exact(b) && !lo)
+          ? mst::exact::launch_flux_update(prec, c->p.flux, c->p.order, dm, a, 0, s)
+          : mst::fast::launch_flux_update(prec, c->p.flux, c->p.order, dm, a, 0, s);
   if (e != cudaSuccess)
     return mst_internal_fail(MST_ECUDA, std::string("residual: ") + cudaGetErrorString(e));
   return MST_OK;
+}
+
+// the residual R(Q) of the current state into ctx->r: while some case is in
+// the FP32 phase, one pass per phase, each skipping the other phase's cases
+// (a case's cells, gradient and faces never mix the two precisions)
+mst_status enqueue_residual(mst_batch* b, int which) {
+  if (!b->lo) return residual_pass(b, which, false, b->ctx->dm);
+  mst::DevMesh dm = b->ctx->dm;
+  dm.case_lo = b->case_lo;
+  dm.lo_want = 1;
+  mst_status st = residual_pass(b, which, true, dm);
+  if (st) return st;
+  dm.lo_want = 0;
+  return residual_pass(b, which, false, dm);
 }
 
 mst::LusgsArgs sweep_args(mst_batch* b, int which) {
@@ -236,8 +253,9 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.n_conv = b->n_conv;
   na.diverged = b->diverged;
   na.iter = b->iter;
-  // the limiter-freezing state machine runs in the FP64 phase only
-  na.frozen = (b->ip.freeze_tol > 0 && !b->lo) ? b->frozen : nullptr;
+  // the limiter-freezing state machine runs in a case's FP64 phase only
+  na.frozen = b->ip.freeze_tol > 0 ? b->frozen : nullptr;
+  na.case_lo = b->lo ? b->case_lo : nullptr;
   na.l2_win = b->l2_win;
   na.own_first = b->own_first;
   na.frz_best = b->frz_best;
@@ -472,6 +490,7 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->norm_part, sizeof(double) * 8 * (size_t)n_cases)) ||
       (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
                                             ? sizeof(float) * 8 * (size_t)nC : 0)) ||
+      (st = balloc(b.get(), &b->case_lo, sizeof(int) * n_cases)) ||
       (st = reset_progress(b.get()))) {
     cleanup();
     return st;
@@ -534,8 +553,11 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   b->first_fixed = false;
   b->lo_best.clear();
   b->lo_best_it.clear();
-  b->lo_ready_max = 0;
-  b->lo_ready_since = 0;
+  if (b->lo) {
+    b->lo_h.assign(b->n_cases, 1);
+    B_CU(cudaMemcpy(b->case_lo, b->lo_h.data(), sizeof(int) * b->n_cases,
+                    cudaMemcpyHostToDevice));
+  }
   if (b->lo || b->sweep32) {
     cudaError_t e = mst::fast::launch_to_f32(b->ctx->q_old, b->ctx->qf_old, b->ctx->dm.n_cells,
                                              b->ctx->stream);
@@ -632,9 +654,9 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     done = h[1];
     if (done >= b->n_cases) break;
     if (b->lo) {
-      // a case is ready to leave the FP32 phase once converged, below
-      // fp32_until, or stagnating in FP32 (its L2 has not fallen by 10%
-      // for win iterations: the FP32 residual's floor)
+      // a case leaves the FP32 phase once converged, below fp32_until, or
+      // stagnating in FP32 (its L2 has not fallen by 10% for win
+      // iterations: the FP32 residual's floor); each case on its own
       B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
@@ -643,30 +665,34 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
         b->lo_best_it.assign(b->n_cases, iters);
       }
       const int win = b->ip.fp32_window > 0 ? b->ip.fp32_window : 500;
-      int ready = 0;
+      int left = 0;
+      bool moved = false;
       for (int i = 0; i < b->n_cases; ++i) {
-        if (cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i]) {
-          ++ready;
-          continue;
+        if (!b->lo_h[i]) continue;
+        bool ready = cv[i] >= 0 || l[i] <= b->ip.fp32_until * f[i];
+        if (!ready) {
+          if (l[i] < 0.9 * b->lo_best[i]) {
+            b->lo_best[i] = l[i];
+            b->lo_best_it[i] = iters;
+          }
+          ready = iters - b->lo_best_it[i] >= win;
         }
-        if (l[i] < 0.9 * b->lo_best[i]) {
-          b->lo_best[i] = l[i];
-          b->lo_best_it[i] = iters;
+        if (ready) {
+          b->lo_h[i] = 0;
+          moved = true;
+        } else {
+          ++left;
         }
-        if (iters - b->lo_best_it[i] >= win) ++ready;
       }
-      if (ready > b->lo_ready_max) {
-        b->lo_ready_max = ready;
-        b->lo_ready_since = iters;
-      }
-      // all ready, or at least half ready and no further case for win
-      // iterations (a case whose FP32 residual oscillates keeps setting
-      // new bests and would hold the whole batch in FP32)
-      if (ready == b->n_cases ||
-          (2 * b->lo_ready_max >= b->n_cases && iters - b->lo_ready_since >= win)) {
+      if (left == 0) {
+        // every case in FP64: the single-phase iterations from here on
         b->lo = false;
         st = ensure_graph();
         if (st) return st;
+      } else if (moved) {
+        // read by the next iterations' launches (same stream)
+        B_CU(cudaMemcpy(b->case_lo, b->lo_h.data(), sizeof(int) * b->n_cases,
+                        cudaMemcpyHostToDevice));
       }
     }
   }

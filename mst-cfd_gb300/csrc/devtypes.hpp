@@ -54,6 +54,12 @@ struct DevMesh {
   // iteration that converged them both state buffers hold the same state.
   const int* c_case;
   const int* case_conv;
+  // batches in mixed precision: each case's residual phase (1: FP32, 0:
+  // FP64) and the phase a launch evaluates; cells of cases in the other
+  // phase are skipped like those of converged cases (nullptr: every case
+  // in the launch's phase)
+  const int* case_lo;
+  int lo_want;
 };
 
 // the cell-face range of device cell c: [3c, 3c + 3) without a load on
@@ -63,17 +69,29 @@ __device__ __forceinline__ int2 cell_face_range(const DevMesh& m, int c) {
   return make_int2(m.c_ptr[c], m.c_ptr[c + 1]);
 }
 
-// true when device cell c belongs to a converged case of a batch
-__device__ __forceinline__ bool cell_case_done(const DevMesh& m, int c) {
-  return m.case_conv && m.case_conv[m.c_case[c]] >= 0;
+// true when case k of a batch is in the other residual phase than the launch
+__device__ __forceinline__ bool case_other_phase(const DevMesh& m, int k) {
+  return m.case_lo && m.case_lo[k] != m.lo_want;
+}
+__device__ __forceinline__ bool cell_other_phase(const DevMesh& m, int c) {
+  return m.case_lo && m.case_lo[m.c_case[c]] != m.lo_want;
 }
 
-// true when every cell of [c0, c1) belongs to a converged case (the cases
-// are contiguous ranges of device cells)
+// true when device cell c belongs to a converged case of a batch, or to a
+// case in the other residual phase
+__device__ __forceinline__ bool cell_case_done(const DevMesh& m, int c) {
+  if (!m.case_conv) return false;
+  const int k = m.c_case[c];
+  return m.case_conv[k] >= 0 || case_other_phase(m, k);
+}
+
+// true when every cell of [c0, c1) belongs to a converged case or to one
+// in the other residual phase (the cases are contiguous ranges of device
+// cells)
 __device__ __forceinline__ bool range_cases_done(const DevMesh& m, int c0, int c1) {
   if (!m.case_conv || c1 <= c0) return false;
   for (int k = m.c_case[c0], e = m.c_case[c1 - 1]; k <= e; ++k)
-    if (m.case_conv[k] < 0) return false;
+    if (m.case_conv[k] < 0 && !case_other_phase(m, k)) return false;
   return true;
 }
 
@@ -203,6 +221,8 @@ struct CaseNormArgs {
   double cfl0, cfl_max, tol, freeze_tol;
   int first_fixed;         // first[] holds reference L2s set by the caller
   double* part;            // [n_cases][8] partial sums of (R_rho / V)^2
+  const int* case_lo;      // [n_cases] 1 while a case's residual is FP32 (the
+                           // freezing state machine waits for FP64), or nullptr
 };
 
 // Precisions / schemes (mirrors of the public enums)

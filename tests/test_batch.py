@@ -297,6 +297,35 @@ def test_gpu_batch_mixed_precision_reaches_tolerance():
 
 
 @pytest.mark.gpu
+def test_gpu_batch_mixed_phases_are_per_case():
+    """Each case leaves the FP32-residual phase on its own: solved in a
+    batch beside cases in either phase, a case ends bit-identical to the
+    same case solved alone with the same options (constant CFL), at the
+    same iteration -- a batch-wide switch would keep the early cases in
+    FP32 until the last one is ready."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    imp = dict(cfl0=50.0, cfl_max=50.0, tol=1e-8, freeze_tol=1e-2, fp32_until=1e-3,
+               fp32_window=100, max_iter=3000)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    b.set_state(q0)
+    r = b.solve()
+    assert r["n_converged"] == len(cases)
+    got, conv = b.state(), b.case_status()["conv_iter"]
+    b.close()
+    for k, (_, mesh, _, cp) in enumerate(cases):
+        one = batch.Batch([(mesh, cp)], implicit=imp, **kw)
+        one.set_state([q0[k]])
+        one.solve()
+        assert np.array_equal(one.state()[0], got[k]), k
+        assert one.case_status()["conv_iter"][0] == conv[k], k
+        one.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("fp32_until", [0.0, 1e-3], ids=["fp64_residual", "mixed_residual"])
 def test_gpu_batch_fp32_sweeps_reach_tolerance(fp32_until):
     """FP32 sweeps (FP64 diagonal inversion and state update): every case
