@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -62,11 +63,12 @@ bool bf16_tile_map(CUtensorMap* map, const void* base, int rows, int K) {
 }
 
 // The persistent TMA kernel where it applies (whole K per CTA, K <= 256 in
-// tiles of 64, at least 17 outputs, 16-byte-aligned operands); false: the
-// caller launches k_gemm_bf16 instead
+// tiles of 64, 16-byte-aligned operands; fewer than 128 outputs use one
+// 128-wide tile whose missing rows of B the copy fills with zeros); false:
+// the caller launches k_gemm_bf16 instead
 bool gemm_tma(const GemmArgs& a, cudaStream_t s, cudaError_t* err) {
   *err = cudaSuccess;
-  if (a.k_chunk > 0 || a.N <= 16 || a.K % kBK != 0 || a.K / kBK > kTmaMaxKT || a.M <= 0 ||
+  if (a.k_chunk > 0 || a.K % kBK != 0 || a.K / kBK > kTmaMaxKT || a.M <= 0 || a.N <= 0 ||
       (reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.B) & 15))
     return false;
   CUtensorMap ma, mb;
@@ -75,20 +77,27 @@ bool gemm_tma(const GemmArgs& a, cudaStream_t s, cudaError_t* err) {
   const int kt = a.K / kBK;
   *err = ensure_smem_limit(k_gemm_tma, tma_smem_bytes(kTmaMaxKT), attr_done);
   if (*err != cudaSuccess) return true;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      sms = 148;
+  // resident CTAs of the device (SMs x CTAs per SM at this K), per K
+  static std::atomic<int> resident[kTmaMaxKT + 1];
+  int slots = resident[kt].load(std::memory_order_relaxed);
+  if (slots <= 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((*err = cudaGetDevice(&dev)) != cudaSuccess ||
+        (*err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) !=
+            cudaSuccess ||
+        (*err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_tma, kTmaThreads,
+                                                              tma_smem_bytes(kt))) != cudaSuccess)
+      return true;
+    slots = std::max(1, sms * per_sm);
+    resident[kt].store(slots, std::memory_order_relaxed);
   }
   TmaGemm t;
   t.g = a;
   t.kt = kt;
   t.n_ntiles = (a.N + kBN - 1) / kBN;
   t.m_tiles = (a.M + kBM - 1) / kBM;
-  // two resident CTAs per SM, each column block with the same number of CTAs
-  int grid = std::min(2 * sms, t.n_ntiles * t.m_tiles);
+  // one wave of resident CTAs, each column block with the same number
+  int grid = std::min(slots, t.n_ntiles * t.m_tiles);
   grid = std::max(t.n_ntiles, grid / t.n_ntiles * t.n_ntiles);
   k_gemm_tma<<<grid, kTmaThreads, tma_smem_bytes(kt), s>>>(ma, mb, t);
   *err = cudaGetLastError();
@@ -104,9 +113,16 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   GemmArgs a = a0;
   const long long lim = g_wait_limit.load(std::memory_order_relaxed);
   a.spin_limit = lim < 0 ? kSpinLimit : (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
-  if (a.lbo == 0) {
+  // MSTCFD_GEMM_TMA=0 keeps every GEMM on k_gemm_bf16 (for comparisons)
+  static const bool use_tma = [] {
+    const char* v = std::getenv("MSTCFD_GEMM_TMA");
+    return !v || std::atoi(v) != 0;
+  }();
+  if (a.lbo == 0 && use_tma) {
     cudaError_t te;
     if (gemm_tma(a, s, &te)) return te;
+  }
+  if (a.lbo == 0) {
     a.lbo = kLBO;
     a.sbo = kSBO;
   }
@@ -158,20 +174,40 @@ __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict
   if (i < n) y[i] = __float2bfloat16_rn(x[i]);
 }
 
-// Z = [bf16(h_c), bf16(mean_{j in N(c)} h_j)] (rows >= n: zero)
-__global__ void k_build_z(const float* __restrict__ h, const int* __restrict__ ptr,
-                          const int* __restrict__ nbr, int n, int n_pad,
-                          __nv_bfloat16* __restrict__ z) {
-  const int c = blockIdx.x, k = threadIdx.x;  // kW threads
-  float a = 0.f, hc = 0.f;
+// Z = [bf16(h_c), bf16(mean_{j in N(c)} h_j)] (rows >= n: zero); one warp
+// per cell, each lane four features (16-byte loads, 8-byte stores), the
+// neighbours summed in list order
+constexpr int kCellsPerBlock = 8;
+__device__ __forceinline__ uint2 bf16x4(float4 v) {
+  const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+  return make_uint2(*reinterpret_cast<const uint32_t*>(&a), *reinterpret_cast<const uint32_t*>(&b));
+}
+__global__ void __launch_bounds__(32 * kCellsPerBlock)
+    k_build_z(const float* __restrict__ h, const int* __restrict__ ptr,
+              const int* __restrict__ nbr, int n, int n_pad, __nv_bfloat16* __restrict__ z) {
+  const int c = blockIdx.x * kCellsPerBlock + (threadIdx.x >> 5), k = (threadIdx.x & 31) * 4;
+  if (c >= n_pad) return;
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f), hc = a;
   if (c < n) {
-    hc = h[(size_t)c * kW + k];
+    hc = *reinterpret_cast<const float4*>(h + (size_t)c * kW + k);
     const int b = ptr[c], e = ptr[c + 1];
-    for (int i = b; i < e; ++i) a += h[(size_t)nbr[i] * kW + k];
-    if (e > b) a /= (float)(e - b);
+    for (int i = b; i < e; ++i) {
+      const float4 v = *reinterpret_cast<const float4*>(h + (size_t)nbr[i] * kW + k);
+      a.x += v.x;
+      a.y += v.y;
+      a.z += v.z;
+      a.w += v.w;
+    }
+    if (e > b) {
+      const float d = (float)(e - b);
+      a.x /= d;
+      a.y /= d;
+      a.z /= d;
+      a.w /= d;
+    }
   }
-  z[(size_t)c * kZ + k] = __float2bfloat16_rn(hc);
-  z[(size_t)c * kZ + kW + k] = __float2bfloat16_rn(a);
+  *reinterpret_cast<uint2*>(z + (size_t)c * kZ + k) = bf16x4(hc);
+  *reinterpret_cast<uint2*>(z + (size_t)c * kZ + kW + k) = bf16x4(a);
 }
 
 // dst[w][n_pad] = transpose of src[n][w] (BF16), zero for rows >= n
@@ -226,19 +262,27 @@ __global__ void k_relu_back(const float* __restrict__ dh, const float* __restric
   dpb[i] = __float2bfloat16_rn(v);
 }
 
-// dH_l = dH_{l+1} + dZ[:, :kW] + sum_{c in N(j)} dZ[c, kW:] / |N(c)|
-__global__ void k_agg_back(const float* __restrict__ dhn, const float* __restrict__ dz,
-                           const int* __restrict__ ptr, const int* __restrict__ nbr, int n,
-                           float* __restrict__ dh) {
-  const int j = blockIdx.x, k = threadIdx.x;
+// dH_l = dH_{l+1} + dZ[:, :kW] + sum_{c in N(j)} dZ[c, kW:] / |N(c)|; one
+// warp per cell, each lane four features, the neighbours in list order
+__global__ void __launch_bounds__(32 * kCellsPerBlock)
+    k_agg_back(const float* __restrict__ dhn, const float* __restrict__ dz,
+               const int* __restrict__ ptr, const int* __restrict__ nbr, int n,
+               float* __restrict__ dh) {
+  const int j = blockIdx.x * kCellsPerBlock + (threadIdx.x >> 5), k = (threadIdx.x & 31) * 4;
   if (j >= n) return;
-  float v = dhn[(size_t)j * kW + k] + dz[(size_t)j * kZ + k];
+  const float4 x = *reinterpret_cast<const float4*>(dhn + (size_t)j * kW + k);
+  const float4 y = *reinterpret_cast<const float4*>(dz + (size_t)j * kZ + k);
+  float4 v = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
   for (int i = ptr[j]; i < ptr[j + 1]; ++i) {
     const int c = nbr[i];
-    const int deg = ptr[c + 1] - ptr[c];
-    v += dz[(size_t)c * kZ + kW + k] / (float)deg;
+    const float deg = (float)(ptr[c + 1] - ptr[c]);
+    const float4 u = *reinterpret_cast<const float4*>(dz + (size_t)c * kZ + kW + k);
+    v.x += u.x / deg;
+    v.y += u.y / deg;
+    v.z += u.z / deg;
+    v.w += u.w / deg;
   }
-  dh[(size_t)j * kW + k] = v;
+  *reinterpret_cast<float4*>(dh + (size_t)j * kW + k) = v;
 }
 
 // Column sums of g[n][w] (bias gradients), w dividing 256, in a fixed order
@@ -486,7 +530,8 @@ cudaError_t forward(mst_mpnn* m, int n) {
   const int np = pad128(n);
   cudaError_t e = gemm(m, m->X, P(m, kWe).wb, m->H[0], np, kW, kInK, kW, P(m, kBe).w, 1, 0);
   for (int l = 0; l < kLayers && e == cudaSuccess; ++l) {
-    k_build_z<<<np, kW>>>(m->H[l], m->ptr, m->nbr, n, np, m->Z[l]);
+    k_build_z<<<(np + kCellsPerBlock - 1) / kCellsPerBlock, 32 * kCellsPerBlock>>>(
+        m->H[l], m->ptr, m->nbr, n, np, m->Z[l]);
     e = cudaMemcpyAsync(m->H[l + 1], m->H[l], sizeof(float) * (size_t)np * kW,
                         cudaMemcpyDeviceToDevice, 0);
     if (e == cudaSuccess)
@@ -551,7 +596,8 @@ cudaError_t backward(mst_mpnn* m, int n, double* loss) {
     if (e == cudaSuccess) e = gemm(m, m->dPb, m->WlT, m->dZ, np, kZ, kW, kZ, nullptr, 0, 0);
     if (e != cudaSuccess) break;
     std::swap(m->dH, m->dHn);  // dHn = dH_{l+1}
-    k_agg_back<<<n, kW>>>(m->dHn, m->dZ, m->ptr, m->nbr, n, m->dH);
+    k_agg_back<<<(n + kCellsPerBlock - 1) / kCellsPerBlock, 32 * kCellsPerBlock>>>(
+        m->dHn, m->dZ, m->ptr, m->nbr, n, m->dH);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) return e;

@@ -148,9 +148,11 @@ struct GemmArgs {
 
 // Epilogue of 16 accumulator columns of one row: bias, ReLU, the residual
 // add (accumulate_c) and the stores of C and its BF16 copy (16-byte stores
-// where the row allows them; vc / vb: C / Cb rows 16-byte aligned).
+// where the row allows them; vc / vb: C / Cb rows 16-byte aligned).  prev:
+// the 16 values of C already loaded for the residual add (or nullptr).
 __device__ __forceinline__ void store16(const GemmArgs& g, bool split, float* Cout, int row,
-                                        int n0, int c0, float v[16], bool vc, bool vb) {
+                                        int n0, int c0, float v[16], bool vc, bool vb,
+                                        const float4* prev = nullptr) {
   if (row < g.M && vc && vb && n0 + c0 + 16 <= g.N) {
     const int col0 = n0 + c0;
 #pragma unroll
@@ -166,7 +168,7 @@ __device__ __forceinline__ void store16(const GemmArgs& g, bool split, float* Co
       for (int j = 0; j < 4; ++j) {
         float4 o = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         if (!split && g.accumulate_c) {
-          const float4 w = p[j];
+          const float4 w = prev ? prev[j] : p[j];
           o.x += w.x;
           o.y += w.y;
           o.z += w.z;

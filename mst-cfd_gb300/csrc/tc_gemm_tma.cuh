@@ -10,8 +10,11 @@
 // own memory, in the 128-byte-swizzled K-major layout, into a ring of
 // kTmaStages stages; warp 1 (one lane) issues tcgen05.mma (kind::f16, BF16 x
 // BF16 -> FP32) into one of two tensor-memory accumulators and commits each
-// stage back to the copier; warps 2-5 read the other accumulator with
-// tcgen05.ld and store the tile, so a tile's epilogue overlaps the next
+// stage back to the copier; warps 2-9 read the other accumulator with
+// tcgen05.ld and store the tile (each warp 32 rows x 64 columns in two
+// loads, released to the MMA thread once both are in registers; whole
+// 32-byte sectors per store; the C values of a residual add loaded before the
+// accumulator is waited for), so a tile's epilogue overlaps the next
 // tile's copies and products.  Every wait is bounded (GemmArgs.spin_limit
 // polls): on timeout a role flags the CTA and the error word, the others
 // stop, the copier waits for its copies in flight and the MMA thread for its
@@ -24,16 +27,18 @@
 namespace mst {
 namespace tc {
 
-constexpr int kTmaStages = 3;                // A ring
-constexpr int kTmaThreads = 192;             // copier, MMA, 4 epilogue warps
+constexpr int kTmaStages = 6;                // A ring
+constexpr int kTmaEpiWarps = 8;              // 4 row quarters x 2 column halves
+constexpr int kTmaThreads = 64 + 32 * kTmaEpiWarps;  // copier, MMA, epilogue
 constexpr int kTmaTile = kBM * kBK * 2;      // one 128-row x 64-K BF16 tile: 16 KB
 constexpr int kTmaMaxKT = 4;                 // K <= 256
 // dynamic shared memory: B (kt tiles) + the A ring + barriers, from a
 // 1024-byte-aligned base (the 128-byte swizzle repeats every 1024 bytes; the
 // kernel checks the base and reports a misaligned one instead of copying);
 // at least 80 KB so that at most two CTAs share an SM (two double
-// accumulators of 128 columns fill its 512 TMEM columns), at most 112.25 KB
-// so that two do
+// accumulators of 128 columns fill its 512 TMEM columns).  The epilogue's
+// registers (the C values of the residual add held across the wait) keep
+// it to one CTA per SM in practice; the launch asks the occupancy.
 __host__ __device__ constexpr int tma_smem_bytes(int kt) {
   return ((kt + kTmaStages) * kTmaTile + 256) < 80 * 1024 ? 80 * 1024
                                                           : (kt + kTmaStages) * kTmaTile + 256;
@@ -79,6 +84,38 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// 32 accumulator columns of this warp's 32 TMEM lanes (one per thread), the
+// load and its completion wait in one statement so that no use of the
+// registers can be scheduled before the wait
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32-byte (one sector) global load / store of 8 floats; the address is
+// 32-byte aligned
+__device__ __forceinline__ void ld8(const float* p, float x[8]) {
+  asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]), "=f"(x[4]), "=f"(x[5]),
+                 "=f"(x[6]), "=f"(x[7])
+               : "l"(p));
+}
+__device__ __forceinline__ void st8(float* p, const float x[8]) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(x[0]),
+               "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7])
+               : "memory");
+}
+
 struct TmaGemm {
   GemmArgs g;
   int kt;        // K / 64
@@ -86,7 +123,7 @@ struct TmaGemm {
   int m_tiles;   // 128-row tiles of M
 };
 
-__global__ void __launch_bounds__(kTmaThreads)
+__global__ void __launch_bounds__(kTmaThreads, 1)
     k_gemm_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const TmaGemm t) {
   constexpr int S = kTmaStages;
@@ -122,7 +159,7 @@ __global__ void __launch_bounds__(kTmaThreads)
     mbar_init(bfull, 1);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
+      mbar_init(&acce[b], kTmaEpiWarps);
     }
     mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -226,14 +263,32 @@ __global__ void __launch_bounds__(kTmaThreads)
       }
     }
   } else {
-    // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4).. = its rows
-    const int q = warp & 3;
+    // epilogue warps 2-9: warp w reads TMEM lanes 32 (w % 4).. (its rows),
+    // columns [64 h, 64 h + 64) with h = (w - 2) / 4
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const int cb = h * (kBN / 2);
     const bool vc = !g.C || ((g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0);
     const bool vb = !g.Cb || ((g.ldcb & 7) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 15) == 0);
+    // whole sectors: C rows 32-byte aligned
+    const bool v32 = !g.C || ((g.ldc & 7) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 31) == 0);
     int i = 0;
     for (int m = m_first; m < t.m_tiles; m += m_step, ++i) {
       const int b = i & 1;
       const uint32_t aph = (uint32_t)(i >> 1) & 1;
+      const int row = m * kBM + q * 32 + lane;
+      // warp-uniform (the TMEM loads below are .sync.aligned): every row of
+      // the warp inside M, all 64 columns inside N, aligned rows
+      const bool fast =
+          __all_sync(0xffffffffu, row < g.M && n0 + cb + kBN / 2 <= g.N && v32 && vb) != 0;
+      // the residual add's C values do not depend on the products: their
+      // loads are in flight while the accumulator is still being formed
+      const bool pre = fast && g.accumulate_c && g.C;
+      float prev[kBN / 2];
+      if (pre) {
+        const float* p = g.C + (size_t)row * g.ldc + n0 + cb;
+#pragma unroll
+        for (int j = 0; j < kBN / 16; ++j) ld8(p + 8 * j, &prev[8 * j]);
+      }
       int go = 0;
       if (lane == 0) go = mbar_wait_or_abort(&accf[b], aph, lim, abort) ? 1 : 0;
       go = __shfl_sync(0xffffffffu, go, 0);
@@ -245,15 +300,61 @@ __global__ void __launch_bounds__(kTmaThreads)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int row = m * kBM + q * 32 + lane;
-      for (int c0 = 0; c0 < kBN; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBN + c0), v);
-        store16(g, false, g.C, row, n0, c0, v, vc, vb);
+      const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBN + cb);
+      if (fast) {
+        const int col0 = n0 + cb;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          float v[32];
+          tmem_ld32(acc + 32 * half, v);
+          if (half == 1) {
+            // the accumulator is in registers: the MMA thread may reuse it
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[b]);
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int c = 32 * half + 8 * j;  // column within the warp's 64
+            float x[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              float y = v[8 * j + k];
+              if (g.bias) y += __ldg(g.bias + col0 + c + k);
+              if (g.relu) y = fmaxf(y, 0.f);
+              x[k] = y;
+            }
+            if (g.C) {
+              float o[8];
+#pragma unroll
+              for (int k = 0; k < 8; ++k) o[k] = pre ? x[k] + prev[c + k] : x[k];
+              st8(g.C + (size_t)row * g.ldc + col0 + c, o);
+            }
+            if (g.Cb) {
+              uint32_t w[4];
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const __nv_bfloat162 b2 = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+                w[k] = *reinterpret_cast<const uint32_t*>(&b2);
+              }
+              *reinterpret_cast<uint4*>(g.Cb + (size_t)row * g.ldcb + col0 + c) =
+                  make_uint4(w[0], w[1], w[2], w[3]);
+            }
+          }
+        }
+      } else {
+        // ragged columns, rows past M or unaligned rows: 16 at a time
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          float v[32];
+          tmem_ld32(acc + 32 * half, v);
+          store16(g, false, g.C, row, n0, cb + 32 * half, &v[0], vc, vb);
+          store16(g, false, g.C, row, n0, cb + 32 * half + 16, &v[16], vc, vb);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[b]);
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acce[b]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

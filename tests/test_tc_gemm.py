@@ -1,10 +1,11 @@
 """The BF16 tensor-core GEMMs (tcgen05, TMEM accumulator) of the learned
 initial field, against an FP32 numpy product of the same BF16 inputs:
 FP32 accumulation, so agreement to a few ulps of FP32 times sqrt(K).  Shapes
-with more than 16 outputs and K <= 256 run the persistent TMA kernel (the
-large ones with several row tiles per CTA, both accumulators and the copy
-ring wrapping), 16 outputs or fewer the 16-wide tile, split K and the
-swapped-stride layout the cp.async kernel."""
+with K <= 256 run the persistent TMA kernel (the large ones with several
+row tiles per CTA, both accumulators and the copy ring wrapping; 4 outputs
+in a 128-wide tile of which the copy fills the rest with zeros); K above
+256, split K and the swapped-stride layout run the cp.async kernel (its
+16-wide tile for 16 outputs or fewer)."""
 import ctypes as C
 
 import numpy as np
@@ -51,7 +52,8 @@ def _run(M, N, K, relu, bias, layout=0, seed=0):
 @pytest.mark.gpu
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 128, 256), (384, 256, 128),
                                    (1000, 4, 128), (130, 128, 64), (89600, 256, 256),
-                                   (40000, 128, 64), (1000, 48, 192)])
+                                   (40000, 128, 64), (1000, 48, 192), (1000, 4, 320),
+                                   (256, 128, 512)])
 @pytest.mark.parametrize("relu,bias", [(0, 0), (1, 1)])
 def test_tc_gemm_matches_numpy(M, N, K, relu, bias):
     from mstcfd import capi
