@@ -415,7 +415,7 @@ def _production(args):
     """Implicit parameters of the batch's production runs (warm start and
     the matching cold start)."""
     return dict(max_iter=args.batch_iters, fp32_until=args.fp32_until, sweep_fp32=1,
-                p_floor=P_FLOOR, fp32_window=args.fp32_window)
+                p_floor=P_FLOOR, fp32_window=args.fp32_window, stall_window=STALL_WINDOW)
 
 
 def _production_label(args):
@@ -424,14 +424,26 @@ def _production_label(args):
             f"sweeps, FP64 diagonal inversion and update")
 
 
-def _batch_solve(cases, q0, imp, grp, l2_ref=None):
+def _case_info(mesh, case):
+    """Cells and flow parameters of one ramp case (mesh, (m, mach, angle, re))."""
+    from mstcfd import meshgen as mg
+    _, mach, angle, re = case
+    return {"cells": int(mesh.n_cells), "mach": round(float(mach), 4),
+            "angle": round(float(angle), 4), "reynolds": round(float(re), 1),
+            "post_shock_mach": round(float(mg.post_shock_mach(mach, angle) or 0.0), 3)}
+
+
+def _batch_solve(cases, q0, imp, grp, l2_ref=None, fallback=None):
     """One batched LU-SGS solve (FP64 production path: Roe + minmod,
-    laminar): wall time (max over ranks), result, per-case status, states."""
+    laminar): wall time (max over ranks), result, per-case status, states.
+    fallback: states a stalled case restarts from within the solve."""
     from mstcfd import batch
     b = batch.Batch(cases, implicit=imp, flux=1, order=2, limiter=1, precision=1, viscous=1)
     b.set_state(q0)
     if l2_ref is not None:
         b.set_l2_ref(l2_ref)
+    if fallback is not None:
+        b.set_fallback(fallback)
     grp.barrier()
     t0 = time.perf_counter()
     r = b.solve()
@@ -444,8 +456,14 @@ def _batch_solve(cases, q0, imp, grp, l2_ref=None):
     return grp.max(wall), r, st, info, q
 
 
+# a case whose L2 has not halved for this many iterations of its FP64 phase
+# is retired as stalled (restarted from the free stream where a warm start
+# set it as the fallback)
+STALL_WINDOW = 3000
+
+
 def _fp64_opts(args):
-    return dict(max_iter=args.batch_iters, p_floor=P_FLOOR)
+    return dict(max_iter=args.batch_iters, p_floor=P_FLOOR, stall_window=STALL_WINDOW)
 
 
 def run_batch(args, ws, rank, grp):
@@ -476,6 +494,7 @@ def run_batch(args, ws, rank, grp):
            "value": round(wall, 3), "device_s": round(r["ms"] * 1e-3, 3),
            "cases": args.batch_cases, "cells": cells_all, "converged": n_conv,
            "diverged": int(grp.sum(r["n_diverged"])),
+           "stalled": int(grp.sum(r["n_stalled"])),
            "partition": "greedy size balancing over ranks, no exchange",
            "iterations": r["iterations"], "max_iter": args.batch_iters,
            "median_case_iterations": int(np.median(conv[conv >= 0])) if (conv >= 0).any() else None,
@@ -487,17 +506,19 @@ def run_batch(args, ws, rank, grp):
                    for (m, _), c in zip(cases, conv)) / (r["ms"] * 1e-3) / 1e6, 1),
            "colors": info["n_colors"], "sweep_threads": info["sweep_threads"],
            "graph_iters": info["graph_iters"],
-           # the cases left at the cap (at most 16): cells and L2 / first L2
-           "not_converged": [{"cells": int(m.n_cells),
-                              "l2_ratio": float(st["last_l2"][i] / st["first_l2"][i])}
-                             for i, (m, _) in enumerate(cases) if conv[i] < 0][:16],
+           # the cases left at the cap (at most 16): cells, flow parameters,
+           # L2 / first L2
+           "not_converged": [dict(_case_info(cases[i][0], fam[i]), case=int(mine[i]),
+                                  l2_ratio=float(st["last_l2"][i] / st["first_l2"][i]))
+                             for i in range(len(cases)) if conv[i] < 0][:16],
            "workload": (f"{len(cases)} compression ramps (no-slip flat plate and ramp), "
                         f"{args.batch_cells[0]}-"
                         f"{args.batch_cells[1]} triangles each, Mach U[1.5,3], angle U[5,15] deg "
                         f"(redrawn while the inviscid post-shock Mach is below 1.2), "
                         f"Re U[1e3,1e4] laminar, Roe + minmod, LU-SGS, temperature floor p >= "
                         f"{P_FLOOR} rho, cap "
-                        f"{args.batch_iters} iterations"),
+                        f"{args.batch_iters} iterations, a case whose L2 has not halved in "
+                        f"{STALL_WINDOW} iterations retired as stalled"),
            "warm": None}
     first_cold = st["first_l2"]
     # the same cold start with the production options
@@ -505,13 +526,14 @@ def run_batch(args, ws, rank, grp):
     cm = stm["conv_iter"]
     out["cold_mixed"] = {"value": round(wall_m, 3), "unit": "s",
                          "converged": int(grp.sum((cm >= 0).sum())),
+                         "stalled": int(grp.sum(rm["n_stalled"])),
                          "iterations": rm["iterations"],
                          "median_case_iterations": int(np.median(cm[cm >= 0]))
                          if (cm >= 0).any() else None,
-                         "not_converged": [{"cells": int(m.n_cells),
-                                            "l2_ratio": float(stm["last_l2"][i]
-                                                              / stm["first_l2"][i])}
-                                           for i, (m, _) in enumerate(cases) if cm[i] < 0][:16],
+                         "not_converged": [dict(_case_info(cases[i][0], fam[i]),
+                                                case=int(mine[i]), l2_ratio=float(stm["last_l2"][i]
+                                                               / stm["first_l2"][i]))
+                                           for i in range(len(cases)) if cm[i] < 0][:16],
                          "precision": _production_label(args)}
     if args.warm_train > 0:
         out["warm"] = run_warm(args, fam, cases, q0, q_cold, conv, first_cold, cm, wall,
@@ -574,11 +596,18 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
     gemm = _gemm_at_scale(net, feats)
     net.close()
 
+    # a warm case that stalls restarts from the free stream inside the
+    # solve (its fallback); its iterations count from the warm start.  (An
+    # iteration budget as the trigger -- restart_after at the 90th
+    # percentile of the training solves' iterations, 10,346 -- restarted
+    # cases that were slow but converging and cost more than it saved.)
+
     def warm_run(opts, conv_c, wall_c, label):
-        wall, r, st, _, qw = _batch_solve(cases, q_warm, opts, grp, l2_ref=first_cold)
+        wall, r, st, _, qw = _batch_solve(cases, q_warm, opts, grp, l2_ref=first_cold,
+                                          fallback=q_free)
         conv = st["conv_iter"]
-        # fallback: cases the warm start did not bring to the tolerance are
-        # solved again from free stream, to the same tolerance
+        # cases still not at the tolerance are solved again from free
+        # stream, to the same tolerance, and that time is added
         miss = [k for k in range(len(cases)) if conv[k] < 0]
         fb_s, fb_conv = 0.0, 0
         if miss:
@@ -595,6 +624,8 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
         res = {"value": round(total, 3), "unit": "s", "precision": label,
                "solve_s": round(wall, 3), "inference_s": round(infer_s, 3),
                "converged": int(grp.sum(n_ok)), "converged_warm": int(grp.sum((conv >= 0).sum())),
+               "restarted_in_solve": int(grp.sum(r["n_restarted"])),
+               "restart_iterations": [int(x) for x in st["restart_iter"] if x >= 0],
                "fallback_cases": len(miss), "fallback_s": round(fb_s, 3),
                "iterations": r["iterations"],
                "iteration_ratio_cold_over_warm": round(float(np.sum(it_c)) / max(np.sum(it_w), 1), 3)

@@ -423,11 +423,23 @@ typedef struct mst_implicit_params {
    * the limiter ratios again from its current state (a limiter frozen on
    * a field still far from the solution can hold a case at a plateau) */
   int refreeze_window;
+  /* stall retirement (0: off): a case whose L2 has not fallen below half
+   * of its best for stall_window iterations of its FP64 phase is retired
+   * (MST_CASE_STALLED) and costs nothing afterwards; if fallback states
+   * are set (mst_batch_set_fallback) it is restarted from its fallback
+   * state instead, once per solve from a set state */
+  int stall_window;
+  /* with fallback states set: a case not converged restart_after
+   * iterations after the state was set restarts from its fallback state,
+   * once (0: off) -- e.g. a warm start held to a budget taken from the
+   * cold-start iterations of its training solves */
+  int restart_after;
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-1,
  * fp32_until 0, max_iter 20000, graph_iters 20, autotune on,
- * sweep_fp32 off, p_floor 0. */
+ * sweep_fp32 off, p_floor 0, refreeze_window 500, stall_window 0,
+ * restart_after 0. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {
@@ -440,6 +452,8 @@ typedef struct mst_batch_result {
   int n_converged;       /* cases at tolerance */
   double ms;             /* device time of the call */
   int n_diverged;        /* cases retired as diverged (MST_CASE_DIVERGED) */
+  int n_stalled;         /* cases retired as stalled (MST_CASE_STALLED) */
+  int n_restarted;       /* cases restarted from their fallback states */
 } mst_batch_result;
 
 /* Joins the meshes into one device mesh (cases keep their cells together)
@@ -469,12 +483,29 @@ mst_status mst_batch_iterate(mst_batch *b, int n);
 mst_status mst_batch_solve(mst_batch *b, mst_batch_result *res);
 /* Per case: the iteration at which it converged (-1: not yet;
  * MST_CASE_DIVERGED: retired because its L2 stopped being finite, which a
- * non-positive density or pressure causes through the sound speed; its
+ * non-positive density or pressure causes through the sound speed;
+ * MST_CASE_STALLED: retired by the stall_window test; a retired case's
  * cells cost nothing from the next iteration on and the other cases run
  * on), the first and the latest L2 (each nullable). */
-enum { MST_CASE_DIVERGED = -2 };
+enum { MST_CASE_DIVERGED = -2, MST_CASE_STALLED = -3 };
 mst_status mst_batch_case_status(mst_batch *b, int *conv_iter,
                                  double *first_l2, double *last_l2);
+/* Fallback states of all cases (the layout of mst_batch_set_state; NULL
+ * clears them), e.g. the free stream behind a learned initial field.  A
+ * case restarted from its fallback state iterates exactly as a solve
+ * started from that state would -- its CFL ramp, limiter freezing,
+ * precision phase and stall test start over; the reference L2 of a
+ * restarted case is its first L2 after the restart unless
+ * mst_batch_set_l2_ref fixed it -- with its iteration numbers shifted by
+ * the iteration of the restart. */
+mst_status mst_batch_set_fallback(mst_batch *b, const double *q);
+/* Restarts the listed cases (indices, each once in the list) from their
+ * fallback states at the current iteration, whatever their status;
+ * MST_EINVAL without fallback states. */
+mst_status mst_batch_restart(mst_batch *b, const int *cases, int n);
+/* Per case the iteration of its latest restart since the state was set,
+ * -1 if none. */
+mst_status mst_batch_case_restarts(mst_batch *b, int *restart_iter);
 
 /* ------------------------------------------------------------------ */
 /* tensor-core GEMM of the learned initial field                       */

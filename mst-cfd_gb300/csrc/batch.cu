@@ -39,21 +39,46 @@ __global__ void k_batch_gather(const double4_32a* __restrict__ src,
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[idx[i]];
 }
-__global__ void k_batch_reset(int n_cases, double cfl0, double* cfl, int* conv_iter,
-                              int* diverged, int* frozen, double* l2_win, int* n_conv,
-                              int* iter) {
+// Per-case progress of a case that (re)starts: all cases with `all`, else
+// those flagged in `flag` (restarts from the fallback states, which also
+// un-count a retired case and start its iteration numbers at *iter).
+struct CaseProgress {
+  double *cfl, *l2_win, *stall_best;
+  int *conv_iter, *diverged, *frozen, *stall_best_it, *restart_it, *n_conv, *iter;
+};
+__global__ void k_batch_reset(int n_cases, double cfl0, CaseProgress p, const int* flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_cases) {
-    cfl[i] = cfl0;
-    conv_iter[i] = -1;
-    diverged[i] = 0;
-    frozen[i] = 0;
-    l2_win[i] = 0.0;
+  const int it = flag ? *p.iter : 0;
+  if (i < n_cases && (!flag || flag[i])) {
+    if (flag && p.conv_iter[i] >= 0) atomicSub(p.n_conv, 1);
+    p.cfl[i] = cfl0;
+    p.conv_iter[i] = -1;
+    p.diverged[i] = 0;
+    p.frozen[i] = 0;
+    p.l2_win[i] = 0.0;
+    p.stall_best[i] = 1e300;
+    p.stall_best_it[i] = it;
+    p.restart_it[i] = it;
   }
-  if (i == 0) {
-    *n_conv = 0;
-    *iter = 0;
+  if (!flag && i == 0) {
+    *p.n_conv = 0;
+    *p.iter = 0;
   }
+}
+
+// the fallback state of every cell of a flagged case into both state
+// buffers (and their FP32 copies where they exist)
+__global__ void k_restart_cells(int n, const int* __restrict__ c_case, const int* __restrict__ flag,
+                                const double4_32a* __restrict__ q_fb, double4_32a* q0,
+                                double4_32a* q1, float4* f0, float4* f1) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n || !flag[c_case[c]]) return;
+  const double4_32a v = q_fb[c];
+  q0[c] = v;
+  q1[c] = v;
+  const float4 f = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+  if (f0) f0[c] = f;
+  if (f1) f1[c] = f;
 }
 
 }  // namespace
@@ -81,6 +106,13 @@ struct mst_batch {
   double* own_first = nullptr;   // per-case L2 of this run's first iteration
   double* frz_best = nullptr;    // per-case best L2 since its limiter froze
   int* frz_best_it = nullptr;
+  double* stall_best = nullptr;  // per-case best L2 of the stall test
+  int* stall_best_it = nullptr;
+  int* restart_it = nullptr;     // per-case iteration of its (re)start
+  int* restart_flag = nullptr;   // per-case flags of one restart call
+  double4_32a* q_fb = nullptr;   // fallback states (device order), or nullptr
+  bool has_fb = false;
+  std::vector<int> restart_iter; // host: per case its restart iteration or -1
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
@@ -261,6 +293,10 @@ mst_status enqueue_iteration(mst_batch* b, int which) {
   na.frz_best = b->frz_best;
   na.frz_best_it = b->frz_best_it;
   na.refreeze_window = b->ip.refreeze_window;
+  na.restart_it = b->restart_it;
+  na.stall_best = b->stall_best;
+  na.stall_best_it = b->stall_best_it;
+  na.stall_window = b->ip.stall_window;
   na.freeze_tol = b->ip.freeze_tol;
   na.first_fixed = b->first_fixed ? 1 : 0;
   na.part = b->norm_part;
@@ -340,11 +376,57 @@ mst_status build_graph(mst_batch* b, int k) {
   return MST_OK;
 }
 
+CaseProgress progress(mst_batch* b) {
+  return CaseProgress{b->cfl,       b->l2_win,        b->stall_best, b->conv_iter,
+                      b->diverged,  b->frozen,        b->stall_best_it,
+                      b->restart_it, b->n_conv,       b->iter};
+}
+
 mst_status reset_progress(mst_batch* b) {
   k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, b->ctx->stream>>>(
-      b->n_cases, b->ip.cfl0, b->cfl, b->conv_iter, b->diverged, b->frozen, b->l2_win,
-      b->n_conv, b->iter);
+      b->n_cases, b->ip.cfl0, progress(b), nullptr);
   B_CU(cudaGetLastError());
+  b->restart_iter.assign(b->n_cases, -1);
+  return MST_OK;
+}
+
+// Restarts the flagged cases from their fallback states at the current
+// iteration: state, per-case progress and (mixed precision) the FP32
+// phase start over.  `iters`: the solve loop's iteration count, for the
+// phase-switch bookkeeping.
+mst_status restart_cases(mst_batch* b, const std::vector<int>& ids, int iters) {
+  mst_ctx* c = b->ctx;
+  std::vector<int> flag(b->n_cases, 0);
+  for (int k : ids) flag[k] = 1;
+  int it = 0;
+  B_CU(cudaMemcpy(&it, b->iter, sizeof(int), cudaMemcpyDeviceToHost));
+  B_CU(cudaMemcpy(b->restart_flag, flag.data(), sizeof(int) * b->n_cases,
+                  cudaMemcpyHostToDevice));
+  const int nC = c->dm.n_cells;
+  k_restart_cells<<<(nC + 255) / 256, 256, 0, c->stream>>>(
+      nC, b->c_case, b->restart_flag, b->q_fb, c->q_old, c->q_new, c->qf_old, c->qf_new);
+  B_CU(cudaGetLastError());
+  k_batch_reset<<<(b->n_cases + 255) / 256, 256, 0, c->stream>>>(
+      b->n_cases, b->ip.cfl0, progress(b), b->restart_flag);
+  B_CU(cudaGetLastError());
+  for (int k : ids) b->restart_iter[k] = it;
+  if (b->ip.fp32_until > 0 && c->p.precision == MST_PREC_FP64) {
+    // the restarted cases begin in the FP32 phase again
+    if (b->lo_h.size() != (size_t)b->n_cases) b->lo_h.assign(b->n_cases, 0);
+    if (b->lo_best.size() != (size_t)b->n_cases) {
+      b->lo_best.assign(b->n_cases, 1e300);
+      b->lo_best_it.assign(b->n_cases, iters);
+    }
+    for (int k : ids) {
+      b->lo_h[k] = 1;
+      b->lo_best[k] = 1e300;
+      b->lo_best_it[k] = iters;
+    }
+    B_CU(cudaMemcpy(b->case_lo, b->lo_h.data(), sizeof(int) * b->n_cases,
+                    cudaMemcpyHostToDevice));
+    b->lo = true;
+  }
+  B_CU(cudaStreamSynchronize(c->stream));
   return MST_OK;
 }
 
@@ -387,11 +469,11 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       !(ip->freeze_tol >= 0) || !(ip->fp32_until >= 0) ||
       (ip->fp32_until > 0 && p->precision == MST_PREC_FP64_EXACT) ||
       ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1) ||
-      ip->refreeze_window < 0)
+      ip->refreeze_window < 0 || ip->stall_window < 0 || ip->restart_after < 0)
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
                              "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0, p_floor >= 0 "
-                             "(0 on the exact path)");
+                             "(0 on the exact path), refreeze_window, stall_window, restart_after >= 0");
   std::unique_ptr<mst_batch> b(new mst_batch());
   b->ip = *ip;
   b->sweep32 = ip->sweep_fp32 != 0 && p->precision != MST_PREC_FP64_EXACT;
@@ -491,6 +573,10 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->grad32, p->precision != MST_PREC_FP32 && ip->fp32_until > 0
                                             ? sizeof(float) * 8 * (size_t)nC : 0)) ||
       (st = balloc(b.get(), &b->case_lo, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->stall_best, sizeof(double) * n_cases)) ||
+      (st = balloc(b.get(), &b->stall_best_it, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->restart_it, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->restart_flag, sizeof(int) * n_cases)) ||
       (st = reset_progress(b.get()))) {
     cleanup();
     return st;
@@ -639,7 +725,7 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   B_CU(cudaEventRecord(c->ev0, c->stream));
   int done = 0, iters = 0;
   std::vector<double> f(b->n_cases), l(b->n_cases);
-  std::vector<int> cv(b->n_cases);
+  std::vector<int> cv(b->n_cases), dv(b->n_cases);
   while (iters < b->ip.max_iter) {
     if (k > 0 && iters + k <= b->ip.max_iter) {
       B_CU(cudaGraphLaunch(b->graph[b->lo ? 1 : 0], c->stream));
@@ -652,6 +738,26 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     B_CU(cudaMemcpyAsync(&h[1], b->n_conv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     B_CU(cudaStreamSynchronize(c->stream));
     done = h[1];
+    const bool stall = b->ip.stall_window > 0 && done > 0;
+    const bool late = b->ip.restart_after > 0 && start + iters >= b->ip.restart_after;
+    if (b->has_fb && (stall || late)) {
+      // a case retired as stalled, or not converged restart_after
+      // iterations after the state was set, restarts from its fallback
+      // state, once
+      B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * dv.size(), cudaMemcpyDeviceToHost));
+      B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
+      std::vector<int> ids;
+      for (int i = 0; i < b->n_cases; ++i)
+        if (b->restart_iter[i] < 0 && ((stall && dv[i] == 2) || (late && cv[i] < 0)))
+          ids.push_back(i);
+      if (!ids.empty()) {
+        st = restart_cases(b, ids, iters);
+        if (st) return st;
+        for (int i : ids) done -= cv[i] >= 0;  // retired cases count again
+        st = ensure_graph();
+        if (st) return st;
+      }
+    }
     if (done >= b->n_cases) break;
     if (b->lo) {
       // a case leaves the FP32 phase once converged, below fp32_until, or
@@ -701,15 +807,20 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   float ms = 0.f;
   B_CU(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   if (res) {
-    std::vector<int> dv(b->n_cases);
     B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * dv.size(), cudaMemcpyDeviceToHost));
-    int n_div = 0;
-    for (int x : dv) n_div += x != 0;
+    int n_div = 0, n_stall = 0, n_rs = 0;
+    for (int x : dv) {
+      n_div += x == 1;
+      n_stall += x == 2;
+    }
+    for (int x : b->restart_iter) n_rs += x >= 0;
     res->iterations = iters;
     res->total_iterations = start + iters;
-    res->n_converged = done - n_div;
+    res->n_converged = done - n_div - n_stall;
     res->ms = ms;
     res->n_diverged = n_div;
+    res->n_stalled = n_stall;
+    res->n_restarted = n_rs;
   }
   return MST_OK;
 }
@@ -723,10 +834,51 @@ mst_status mst_batch_case_status(mst_batch* b, int* conv_iter, double* first_l2,
     B_CU(cudaMemcpy(conv_iter, b->conv_iter, sizeof(int) * n, cudaMemcpyDeviceToHost));
     B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * n, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < n; ++i)
-      if (dv[i]) conv_iter[i] = MST_CASE_DIVERGED;
+      if (dv[i]) conv_iter[i] = dv[i] == 2 ? MST_CASE_STALLED : MST_CASE_DIVERGED;
   }
   if (first_l2) B_CU(cudaMemcpy(first_l2, b->first, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (last_l2) B_CU(cudaMemcpy(last_l2, b->last, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return MST_OK;
+}
+
+mst_status mst_batch_set_fallback(mst_batch* b, const double* q) {
+  if (!b) return mst_internal_fail(MST_EINVAL, "NULL batch");
+  if (!q) {
+    b->has_fb = false;
+    return MST_OK;
+  }
+  mst_ctx* c = b->ctx;
+  const int nC = c->dm.n_cells;
+  mst_status st = MST_OK;
+  if (!b->q_fb && (st = balloc(b, &b->q_fb, sizeof(double4_32a) * (size_t)nC))) return st;
+  // host rows (file order) -> device order, through the context's staging
+  B_CU(cudaMemcpyAsync(c->stage_in, q, sizeof(double4_32a) * (size_t)nC, cudaMemcpyHostToDevice,
+                       c->stream));
+  k_batch_gather<<<(nC + 255) / 256, 256, 0, c->stream>>>(c->stage_in, c->d.cell_iperm, b->q_fb,
+                                                           nC);
+  B_CU(cudaGetLastError());
+  B_CU(cudaStreamSynchronize(c->stream));
+  b->has_fb = true;
+  return MST_OK;
+}
+
+mst_status mst_batch_restart(mst_batch* b, const int* cases, int n) {
+  if (!b || (n > 0 && !cases) || n < 0) return mst_internal_fail(MST_EINVAL, "bad argument");
+  if (!b->has_fb) return mst_internal_fail(MST_EINVAL, "no fallback states (mst_batch_set_fallback)");
+  std::vector<int> ids(cases, cases + n);
+  std::vector<char> seen(b->n_cases, 0);
+  for (int k : ids) {
+    if (k < 0 || k >= b->n_cases || seen[k])
+      return mst_internal_fail(MST_EINVAL, "case index out of range or repeated");
+    seen[k] = 1;
+  }
+  if (ids.empty()) return MST_OK;
+  return restart_cases(b, ids, 0);
+}
+
+mst_status mst_batch_case_restarts(mst_batch* b, int* restart_iter) {
+  if (!b || !restart_iter) return mst_internal_fail(MST_EINVAL, "NULL argument");
+  std::memcpy(restart_iter, b->restart_iter.data(), sizeof(int) * b->n_cases);
   return MST_OK;
 }
 

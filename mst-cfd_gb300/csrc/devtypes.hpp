@@ -223,6 +223,10 @@ struct CaseNormArgs {
   double* part;            // [n_cases][8] partial sums of (R_rho / V)^2
   const int* case_lo;      // [n_cases] 1 while a case's residual is FP32 (the
                            // freezing state machine waits for FP64), or nullptr
+  const int* restart_it;   // [n_cases] iteration of the case's (re)start
+  double* stall_best;      // [n_cases] best L2 of the stall test
+  int* stall_best_it;      // [n_cases] and its iteration
+  int stall_window;        // see mst_implicit_params (0: off)
 };
 
 // Precisions / schemes (mirrors of the public enums)

@@ -79,6 +79,20 @@ class Batch:
         r = capi.f64(np.asarray(l2_ref, np.float64), (len(self.meshes),))
         capi.check(capi.load().mst_batch_set_l2_ref(self._h, capi.dptr(r)))
 
+    def set_fallback(self, states):
+        """Fallback state of every case (list of arrays, as set_state), or
+        None: with stall_window set, a stalled case restarts from it."""
+        if states is None:
+            capi.check(capi.load().mst_batch_set_fallback(self._h, None))
+            return
+        q = capi.f64(np.concatenate(states, 0), (int(self.case_cells[-1]), 4))
+        capi.check(capi.load().mst_batch_set_fallback(self._h, capi.dptr(q)))
+
+    def restart(self, cases):
+        """Restart the listed cases from their fallback states now."""
+        ids = np.ascontiguousarray(cases, dtype=np.int32)
+        capi.check(capi.load().mst_batch_restart(self._h, ids.ctypes.data_as(capi._ip), len(ids)))
+
     def state(self):
         q = np.zeros((int(self.case_cells[-1]), 4))
         capi.check(capi.load().mst_batch_get_state(self._h, capi.dptr(q)))
@@ -98,7 +112,9 @@ class Batch:
         f, l = np.zeros(n), np.zeros(n)
         capi.check(capi.load().mst_batch_case_status(
             self._h, it.ctypes.data_as(capi._ip), capi.dptr(f), capi.dptr(l)))
-        return dict(conv_iter=it, first_l2=f, last_l2=l)
+        rs = np.zeros(n, np.int32)
+        capi.check(capi.load().mst_batch_case_restarts(self._h, rs.ctypes.data_as(capi._ip)))
+        return dict(conv_iter=it, first_l2=f, last_l2=l, restart_iter=rs)
 
     def close(self):
         h = getattr(self, "_h", None)

@@ -80,7 +80,8 @@ class ImplicitParams(C.Structure):
                 ("tol", C.c_double), ("freeze_tol", C.c_double), ("fp32_until", C.c_double),
                 ("max_iter", C.c_int), ("graph_iters", C.c_int),
                 ("autotune", C.c_int), ("sweep_fp32", C.c_int), ("p_floor", C.c_double),
-                ("fp32_window", C.c_int), ("refreeze_window", C.c_int)]
+                ("fp32_window", C.c_int), ("refreeze_window", C.c_int),
+                ("stall_window", C.c_int), ("restart_after", C.c_int)]
 
 
 class BatchInfo(C.Structure):
@@ -90,10 +91,12 @@ class BatchInfo(C.Structure):
 
 class BatchResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("total_iterations", C.c_int),
-                ("n_converged", C.c_int), ("ms", C.c_double), ("n_diverged", C.c_int)]
+                ("n_converged", C.c_int), ("ms", C.c_double), ("n_diverged", C.c_int),
+                ("n_stalled", C.c_int), ("n_restarted", C.c_int)]
 
 
 CASE_DIVERGED = -2  # mst_batch_case_status: the case was retired as diverged
+CASE_STALLED = -3   # ... retired by the stall_window test
 
 
 class MeshInfo(C.Structure):
@@ -214,6 +217,9 @@ def load():
         "mst_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
         "mst_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(BatchResult)]),
         "mst_batch_case_status": (C.c_int, [C.c_void_p, _ip, _dp, _dp]),
+        "mst_batch_set_fallback": (C.c_int, [C.c_void_p, _dp]),
+        "mst_batch_restart": (C.c_int, [C.c_void_p, _ip, C.c_int]),
+        "mst_batch_case_restarts": (C.c_int, [C.c_void_p, _ip]),
         "mst_tc_gemm_check": (C.c_int, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_float),
                                         C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int]),

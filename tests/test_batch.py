@@ -326,6 +326,104 @@ def test_gpu_batch_mixed_phases_are_per_case():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("fp32", [0.0, 1e-3], ids=["fp64", "mixed"])
+def test_gpu_batch_restart_from_fallback_is_a_cold_start(fp32):
+    """A case restarted from its fallback state iterates exactly as a solve
+    started from it: case 1 starts from a perturbed state, restarts from
+    the free stream after 40 iterations, and ends bit-identical to the
+    cold start's case 1, 40 iterations later; the other cases are
+    untouched."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    imp = dict(tol=1e-8, freeze_tol=0.1, fp32_until=fp32, fp32_window=100, max_iter=4000)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    cold = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    cold.set_state(q0)
+    cold.solve()
+    qc, cc = cold.state(), cold.case_status()["conv_iter"]
+    cold.close()
+    assert np.all(cc >= 0)
+    bad = [q.copy() for q in q0]
+    bad[1] = bad[1] * np.array([1.1, 0.9, 1.0, 1.05])
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    b.set_state(bad)
+    b.set_fallback(q0)
+    b.iterate(40)
+    b.restart([1])
+    r = b.solve()
+    st, qb = b.case_status(), b.state()
+    b.close()
+    assert r["n_restarted"] == 1 and list(st["restart_iter"]) == [-1, 40, -1]
+    assert st["conv_iter"][1] == cc[1] + 40
+    for k in range(len(cases)):
+        assert np.array_equal(qb[k], qc[k]), k
+
+
+@pytest.mark.gpu
+def test_gpu_batch_restart_after_an_iteration_budget():
+    """restart_after: every case not converged 40 iterations after the
+    state was set restarts from its fallback state at the next graph
+    launch boundary, once, and then iterates as a cold start would (final
+    states bit-identical, convergence 40 iterations later)."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    imp = dict(tol=1e-8, freeze_tol=0.1, max_iter=4000, graph_iters=20)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    cold = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=imp, **kw)
+    cold.set_state(q0)
+    cold.solve()
+    qc, cc = cold.state(), cold.case_status()["conv_iter"]
+    cold.close()
+    bad = [q * np.array([1.1, 0.9, 1.0, 1.05]) for q in q0]
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                    implicit=dict(imp, restart_after=40), **kw)
+    b.set_state(bad)
+    b.set_fallback(q0)
+    r = b.solve()
+    st, qb = b.case_status(), b.state()
+    b.close()
+    assert r["n_restarted"] == len(cases) and np.all(st["restart_iter"] == 40)
+    assert np.array_equal(st["conv_iter"], cc + 40)
+    for k in range(len(cases)):
+        assert np.array_equal(qb[k], qc[k]), k
+
+
+@pytest.mark.gpu
+def test_gpu_batch_stalled_cases_retire_or_restart_once():
+    """The stall test: with a 2-iteration window every case stalls within a
+    few graph launches and is retired (MST_CASE_STALLED, no further cost);
+    with fallback states each case first restarts from them, once, then
+    stalls again."""
+    from mstcfd import batch, capi
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                    implicit=dict(stall_window=2, max_iter=4000),
+                    flux=1, order=2, limiter=1, precision=1)
+    b.set_state(q0)
+    r = b.solve()
+    st = b.case_status()
+    assert r["n_stalled"] == len(cases) and r["n_converged"] == 0 and r["n_restarted"] == 0
+    assert np.all(st["conv_iter"] == capi.CASE_STALLED) and r["iterations"] < 500
+    assert np.all(st["restart_iter"] == -1)
+    b.set_state(q0)
+    b.set_fallback(q0)
+    r = b.solve()
+    st = b.case_status()
+    assert r["n_restarted"] == len(cases) and r["n_stalled"] == len(cases)
+    assert np.all(st["restart_iter"] > 0) and r["iterations"] < 1000
+    with pytest.raises(capi.MstError):
+        b.set_fallback(None)
+        b.restart([0])
+    b.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("fp32_until", [0.0, 1e-3], ids=["fp64_residual", "mixed_residual"])
 def test_gpu_batch_fp32_sweeps_reach_tolerance(fp32_until):
     """FP32 sweeps (FP64 diagonal inversion and state update): every case
