@@ -113,6 +113,15 @@ struct mst_batch {
   double4_32a* q_fb = nullptr;   // fallback states (device order), or nullptr
   bool has_fb = false;
   std::vector<int> restart_iter; // host: per case its restart iteration or -1
+  // compaction: once most cases have converged, the residual kernels visit
+  // the tiles and the sweeps the cells of unconverged cases only
+  std::vector<int> c_case_h;     // case of every device cell
+  std::vector<int> color_cells_h;
+  int* tile_list = nullptr;      // device [n_tiles]
+  int* act_cells = nullptr;      // device [n_cells]: per colour, active cells
+  std::vector<int> act_off;      // [n_colors + 1] into act_cells
+  bool compact = false;          // lists in use
+  long long list_cells = 0;      // cells of the cases the lists hold
   void* phi = nullptr;           // recorded limiter ratios [n_faces][2][4]
   double4_32a* dq = nullptr;
   double* diag = nullptr;
@@ -255,8 +264,10 @@ mst_status enqueue_sweeps(mst_batch* b, int which, int threads) {
     for (int i = 0; i < b->n_colors; ++i) {
       const int col = pass == 0 ? i : b->n_colors - 1 - i;
       la.col = col;
-      la.cells = b->color_cells + b->color_off[col];
-      la.n = b->color_off[col + 1] - b->color_off[col];
+      const int* cells = b->compact ? b->act_cells : b->color_cells;
+      const std::vector<int>& off = b->compact ? b->act_off : b->color_off;
+      la.cells = cells + off[col];
+      la.n = off[col + 1] - off[col];
       cudaError_t e;
       if (pass == 0)
         e = exact(b) ? mst::exact::lusgs_forward_t(c->dm, la, threads, c->stream)
@@ -430,6 +441,64 @@ mst_status restart_cases(mst_batch* b, const std::vector<int>& ids, int iters) {
   return MST_OK;
 }
 
+void drop_graphs(mst_batch* b) {
+  for (int i = 0; i < 2; ++i)
+    if (b->graph[i]) {
+      cudaGraphExecDestroy(b->graph[i]);
+      b->graph[i] = nullptr;
+    }
+}
+
+// Lists of the tiles and (per colour) cells of the cases with cv < 0; the
+// graphs hold the launches' grids, so they are captured again.
+mst_status build_lists(mst_batch* b, const std::vector<int>& cv) {
+  mst_ctx* c = b->ctx;
+  const int nC = c->dm.n_cells, nT = c->dm.n_tiles;
+  std::vector<int> tiles;
+  tiles.reserve(nT);
+  for (int t = 0; t < nT; ++t) {
+    const int k0 = b->c_case_h[t * mst::kTileCells];
+    const int k1 = b->c_case_h[std::min((t + 1) * mst::kTileCells, nC) - 1];
+    for (int k = k0; k <= k1; ++k)
+      if (cv[k] < 0) {
+        tiles.push_back(t);
+        break;
+      }
+  }
+  std::vector<int> cells;
+  cells.reserve(nC);
+  b->act_off.assign(b->n_colors + 1, 0);
+  for (int col = 0; col < b->n_colors; ++col) {
+    for (int i = b->color_off[col]; i < b->color_off[col + 1]; ++i) {
+      const int d = b->color_cells_h[i];
+      if (cv[b->c_case_h[d]] < 0) cells.push_back(d);
+    }
+    b->act_off[col + 1] = (int)cells.size();
+  }
+  if (!tiles.empty())
+    B_CU(cudaMemcpy(b->tile_list, tiles.data(), sizeof(int) * tiles.size(),
+                    cudaMemcpyHostToDevice));
+  if (!cells.empty())
+    B_CU(cudaMemcpy(b->act_cells, cells.data(), sizeof(int) * cells.size(),
+                    cudaMemcpyHostToDevice));
+  c->dm.tile_list = b->tile_list;
+  c->dm.n_list = (int)tiles.size();
+  b->compact = true;
+  b->list_cells = (long long)cells.size();
+  drop_graphs(b);
+  return MST_OK;
+}
+
+// back to launches over every tile and cell
+void full_lists(mst_batch* b) {
+  if (!b->compact) return;
+  b->ctx->dm.tile_list = nullptr;
+  b->ctx->dm.n_list = 0;
+  b->compact = false;
+  b->list_cells = b->ctx->dm.n_cells;
+  drop_graphs(b);
+}
+
 mst_status run_iterations(mst_batch* b, int n) {
   for (int i = 0; i < n; ++i) {
     mst_status st = enqueue_iteration(b, b->cur);
@@ -577,6 +646,8 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       (st = balloc(b.get(), &b->stall_best_it, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->restart_it, sizeof(int) * n_cases)) ||
       (st = balloc(b.get(), &b->restart_flag, sizeof(int) * n_cases)) ||
+      (st = balloc(b.get(), &b->tile_list, sizeof(int) * (size_t)L.n_tiles)) ||
+      (st = balloc(b.get(), &b->act_cells, sizeof(int) * (size_t)nC)) ||
       (st = reset_progress(b.get()))) {
     cleanup();
     return st;
@@ -584,6 +655,9 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
   // the residual kernels skip the cells of converged cases
   b->ctx->dm.c_case = b->c_case;
   b->ctx->dm.case_conv = b->conv_iter;
+  b->c_case_h = std::move(c_case);
+  b->color_cells_h = std::move(cells);
+  b->list_cells = nC;
   if (cudaStreamSynchronize(b->ctx->stream) != cudaSuccess) {
     cleanup();
     return mst_internal_fail(MST_ECUDA, "batch setup failed");
@@ -625,6 +699,7 @@ mst_status mst_batch_set_state(mst_batch* b, const double* q) {
   if (!b || !q) return mst_internal_fail(MST_EINVAL, "NULL argument");
   mst_status st = mst_set_state(b->ctx, q, 4);
   if (st) return st;
+  full_lists(b);
   b->cur = 0;
   // a new solve starts in the FP32-residual phase when one is configured
   b->lo = b->ip.fp32_until > 0 && b->ctx->p.precision == MST_PREC_FP64;
@@ -723,9 +798,10 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   B_CU(cudaMemcpy(&h[0], b->iter, sizeof(int), cudaMemcpyDeviceToHost));
   const int start = h[0];
   B_CU(cudaEventRecord(c->ev0, c->stream));
-  int done = 0, iters = 0;
+  int done = 0, iters = 0, last_done = 0;
   std::vector<double> f(b->n_cases), l(b->n_cases);
   std::vector<int> cv(b->n_cases), dv(b->n_cases);
+  const std::vector<int>& case_cells = b->mesh->host.case_cells;
   while (iters < b->ip.max_iter) {
     if (k > 0 && iters + k <= b->ip.max_iter) {
       B_CU(cudaGraphLaunch(b->graph[b->lo ? 1 : 0], c->stream));
@@ -738,6 +814,7 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     B_CU(cudaMemcpyAsync(&h[1], b->n_conv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     B_CU(cudaStreamSynchronize(c->stream));
     done = h[1];
+    bool restarted = false;
     const bool stall = b->ip.stall_window > 0 && done > 0;
     const bool late = b->ip.restart_after > 0 && start + iters >= b->ip.restart_after;
     if (b->has_fb && (stall || late)) {
@@ -753,12 +830,33 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
       if (!ids.empty()) {
         st = restart_cases(b, ids, iters);
         if (st) return st;
-        for (int i : ids) done -= cv[i] >= 0;  // retired cases count again
+        for (int i : ids) {
+          done -= cv[i] >= 0;  // retired cases count again
+          cv[i] = -1;
+        }
+        restarted = true;
         st = ensure_graph();
         if (st) return st;
       }
     }
     if (done >= b->n_cases) break;
+    if (done != last_done || restarted) {
+      // compaction: once the unconverged cases hold at most 3/4 of the
+      // cells the launches cover, the lists shrink to theirs (a restarted
+      // case must be in them again)
+      if (!restarted)
+        B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
+      long long act = 0;
+      for (int i = 0; i < b->n_cases; ++i)
+        if (cv[i] < 0) act += case_cells[i + 1] - case_cells[i];
+      if ((restarted && b->compact) || 4 * act <= 3 * b->list_cells) {
+        st = build_lists(b, cv);
+        if (st) return st;
+        st = ensure_graph();
+        if (st) return st;
+      }
+      last_done = done;
+    }
     if (b->lo) {
       // a case leaves the FP32 phase once converged, below fp32_until, or
       // stagnating in FP32 (its L2 has not fallen by 10% for win
@@ -873,6 +971,8 @@ mst_status mst_batch_restart(mst_batch* b, const int* cases, int n) {
     seen[k] = 1;
   }
   if (ids.empty()) return MST_OK;
+  // launches over every tile again (the solve compacts them anew)
+  full_lists(b);
   return restart_cases(b, ids, 0);
 }
 

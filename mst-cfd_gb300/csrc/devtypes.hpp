@@ -60,6 +60,10 @@ struct DevMesh {
   // in the launch's phase)
   const int* case_lo;
   int lo_want;
+  // batches: the tiles the residual kernels visit (those holding cells of
+  // unconverged cases) when most cases have converged; nullptr: all tiles
+  const int* tile_list;
+  int n_list;
 };
 
 // the cell-face range of device cell c: [3c, 3c + 3) without a load on
