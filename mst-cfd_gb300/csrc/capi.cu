@@ -1090,6 +1090,10 @@ mst_status enqueue_steps(mst_ctx* c, int nsteps, double t_end, bool last_norms =
 }
 
 // ---- host-buffer pipeline ----
+__global__ void k_copy_doubles(const double* __restrict__ src, double* __restrict__ dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
 __global__ void k_load_rows(const double4_32a* __restrict__ src, const int* __restrict__ iperm,
                             double4_32a* __restrict__ q, float4* __restrict__ hi,
                             float4* __restrict__ lo, int n) {
@@ -1186,8 +1190,12 @@ mst_status mst_step_host_jobs(mst_ctx* c, int n_jobs, const double* const* q_in,
     c->grad_valid = false;
     st = enqueue_steps(c, nsteps, 0.0);
     if (st) return st;
-    CU(cudaMemcpyAsync(P.job_norms + (size_t)j * (kNormSlots + 2), c->norms,
-                       sizeof(double) * (kNormSlots + 2), cudaMemcpyDeviceToDevice, c->stream));
+    // the job's norms kept for the divergence check: a one-warp copy (a
+    // device-to-device cudaMemcpyAsync would go through a copy engine and
+    // could queue behind the other jobs' 64 MB host transfers)
+    k_copy_doubles<<<1, 32, 0, c->stream>>>(c->norms, P.job_norms + (size_t)j * (kNormSlots + 2),
+                                            kNormSlots + 2);
+    CU(cudaGetLastError());
     // state -> out slot in file order (after the slot's previous job left)
     CU(cudaStreamWaitEvent(c->stream, P.out_free[k], 0));
     if (fp32)
@@ -1196,7 +1204,7 @@ mst_status mst_step_host_jobs(mst_ctx* c, int n_jobs, const double* const* q_in,
     else
       k_gather_rows<<<nb, 256, 0, c->stream>>>(c->q_old, c->d.cell_perm, P.slot_out[k], nC);
     CU(cudaGetLastError());
-    c->last_launches += 2;
+    c->last_launches += 3;
     CU(cudaEventRecord(P.out_ready[k], c->stream));
     // out: slot -> host
     CU(cudaStreamWaitEvent(P.out, P.out_ready[k], 0));
