@@ -603,8 +603,10 @@ def run_warm(args, fam, cases, q_free, q_cold, conv_cold, first_cold, conv_cold_
     # cases that were slow but converging and cost more than it saved.)
 
     def warm_run(opts, conv_c, wall_c, label):
-        wall, r, st, _, qw = _batch_solve(cases, q_warm, opts, grp, l2_ref=first_cold,
-                                          fallback=q_free)
+        # ... or whose L2, at its rate over two 1,000-iteration windows in a
+        # row, would not reach the tolerance within the cap
+        wall, r, st, _, qw = _batch_solve(cases, q_warm, dict(opts, restart_projected=1000),
+                                          grp, l2_ref=first_cold, fallback=q_free)
         conv = st["conv_iter"]
         # cases still not at the tolerance are solved again from free
         # stream, to the same tolerance, and that time is added

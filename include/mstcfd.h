@@ -434,12 +434,20 @@ typedef struct mst_implicit_params {
    * once (0: off) -- e.g. a warm start held to a budget taken from the
    * cold-start iterations of its training solves */
   int restart_after;
+  /* with fallback states set: every restart_projected iterations after
+   * the state was set, a case whose L2, extrapolated at its rate over the
+   * last window, would not reach the tolerance within max_iter -- in two
+   * windows in a row, counted in its FP64 phase -- restarts from its
+   * fallback state, once (0: off): a slow warm start gives way to the
+   * free stream while a slow case that will still make the cap is left
+   * alone */
+  int restart_projected;
 } mst_implicit_params;
 
 /* cfl0 50, cfl_max 100, omega 1.2, tol 1e-8, freeze_tol 1e-1,
  * fp32_until 0, max_iter 20000, graph_iters 20, autotune on,
  * sweep_fp32 off, p_floor 0, refreeze_window 500, stall_window 0,
- * restart_after 0. */
+ * restart_after 0, restart_projected 0. */
 void mst_implicit_params_default(mst_implicit_params *p);
 
 typedef struct mst_batch_info_t {

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -538,11 +539,13 @@ mst_status mst_batch_create(const mst_mesh* const* meshes, const mst_case_params
       !(ip->freeze_tol >= 0) || !(ip->fp32_until >= 0) ||
       (ip->fp32_until > 0 && p->precision == MST_PREC_FP64_EXACT) ||
       ip->max_iter < 0 || ip->graph_iters < 0 || (ip->graph_iters & 1) ||
-      ip->refreeze_window < 0 || ip->stall_window < 0 || ip->restart_after < 0)
+      ip->refreeze_window < 0 || ip->stall_window < 0 || ip->restart_after < 0 ||
+      ip->restart_projected < 0)
     return mst_internal_fail(MST_EINVAL,
                              "implicit parameters: need cfl0 > 0, cfl_max >= cfl0, omega >= 1, "
                              "tol > 0, max_iter >= 0, graph_iters >= 0 and even, fp32_until >= 0, p_floor >= 0 "
-                             "(0 on the exact path), refreeze_window, stall_window, restart_after >= 0");
+                             "(0 on the exact path), refreeze_window, stall_window, restart_after, "
+                             "restart_projected >= 0");
   std::unique_ptr<mst_batch> b(new mst_batch());
   b->ip = *ip;
   b->sweep32 = ip->sweep_fp32 != 0 && p->precision != MST_PREC_FP64_EXACT;
@@ -799,6 +802,11 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
   const int start = h[0];
   B_CU(cudaEventRecord(c->ev0, c->stream));
   int done = 0, iters = 0, last_done = 0;
+  // restart_projected: per case the L2 at the start of the current window
+  const int pw = b->ip.restart_projected;
+  std::vector<double> proj_l2(b->n_cases, -1.0);
+  std::vector<int> proj_slow(b->n_cases, 0);
+  int next_proj = pw > 0 ? pw : 0;
   std::vector<double> f(b->n_cases), l(b->n_cases);
   std::vector<int> cv(b->n_cases), dv(b->n_cases);
   const std::vector<int>& case_cells = b->mesh->host.case_cells;
@@ -815,17 +823,48 @@ mst_status mst_batch_solve(mst_batch* b, mst_batch_result* res) {
     B_CU(cudaStreamSynchronize(c->stream));
     done = h[1];
     bool restarted = false;
+    const int now = start + iters;  // iterations since the state was set
     const bool stall = b->ip.stall_window > 0 && done > 0;
-    const bool late = b->ip.restart_after > 0 && start + iters >= b->ip.restart_after;
-    if (b->has_fb && (stall || late)) {
-      // a case retired as stalled, or not converged restart_after
-      // iterations after the state was set, restarts from its fallback
-      // state, once
+    const bool late = b->ip.restart_after > 0 && now >= b->ip.restart_after;
+    const bool proj = pw > 0 && now >= next_proj;
+    if (b->has_fb && (stall || late || proj)) {
+      // a case retired as stalled, not converged restart_after iterations
+      // after the state was set, or projected past max_iter restarts from
+      // its fallback state, once
       B_CU(cudaMemcpy(dv.data(), b->diverged, sizeof(int) * dv.size(), cudaMemcpyDeviceToHost));
       B_CU(cudaMemcpy(cv.data(), b->conv_iter, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost));
+      std::vector<char> slow(b->n_cases, 0);
+      if (proj) {
+        B_CU(cudaMemcpy(f.data(), b->first, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
+        B_CU(cudaMemcpy(l.data(), b->last, sizeof(double) * l.size(), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < b->n_cases; ++i) {
+          if (b->lo && b->lo_h[i]) {
+            // the FP32 phase levels off by design: the window starts
+            // when the case leaves it
+            proj_l2[i] = -1.0;
+            continue;
+          }
+          if (cv[i] < 0 && b->restart_iter[i] < 0 && proj_l2[i] > 0.0 && l[i] > 0.0 &&
+              f[i] > 0.0) {
+            // iterations still needed at the last window's rate (decades
+            // per iteration); no progress projects to infinity.  Two
+            // windows in a row (a plateau before the limiter freezes is
+            // not a slow case)
+            const double rate = std::log10(proj_l2[i] / l[i]) / pw;
+            const double need = std::log10(l[i] / (b->ip.tol * f[i]));
+            const bool past =
+                need > 0.0 && (rate <= 0.0 || now + need / rate > (double)b->ip.max_iter);
+            proj_slow[i] = past ? proj_slow[i] + 1 : 0;
+            slow[i] = proj_slow[i] >= 2;
+          }
+          proj_l2[i] = l[i];
+        }
+        next_proj = now + pw;
+      }
       std::vector<int> ids;
       for (int i = 0; i < b->n_cases; ++i)
-        if (b->restart_iter[i] < 0 && ((stall && dv[i] == 2) || (late && cv[i] < 0)))
+        if (b->restart_iter[i] < 0 &&
+            ((stall && dv[i] == 2) || (late && cv[i] < 0) || (slow[i] && cv[i] < 0)))
           ids.push_back(i);
       if (!ids.empty()) {
         st = restart_cases(b, ids, iters);

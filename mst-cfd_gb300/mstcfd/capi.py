@@ -81,7 +81,8 @@ class ImplicitParams(C.Structure):
                 ("max_iter", C.c_int), ("graph_iters", C.c_int),
                 ("autotune", C.c_int), ("sweep_fp32", C.c_int), ("p_floor", C.c_double),
                 ("fp32_window", C.c_int), ("refreeze_window", C.c_int),
-                ("stall_window", C.c_int), ("restart_after", C.c_int)]
+                ("stall_window", C.c_int), ("restart_after", C.c_int),
+                ("restart_projected", C.c_int)]
 
 
 class BatchInfo(C.Structure):

@@ -393,6 +393,39 @@ def test_gpu_batch_restart_after_an_iteration_budget():
 
 
 @pytest.mark.gpu
+def test_gpu_batch_restart_when_projected_past_the_cap():
+    """restart_projected: with a tolerance no case can reach in 400
+    iterations (1e-30), every case projects past the cap in the windows
+    ending at iterations 80 and 120 and restarts from its fallback state at
+    120; at the cap its state equals a cold start's after 280 iterations,
+    bit for bit."""
+    from mstcfd import batch
+    from mstcfd import meshgen as mg
+    cases = _batch_cases(0)
+    imp = dict(tol=1e-30, freeze_tol=0.1, graph_iters=20)
+    kw = dict(flux=1, order=2, limiter=1, precision=1)
+    q0 = [mg.freestream(mach, mesh.n_cells) for _, mesh, mach, _ in cases]
+    cold = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases], implicit=dict(imp, max_iter=280),
+                       **kw)
+    cold.set_state(q0)
+    cold.solve()
+    qc = cold.state()
+    cold.close()
+    bad = [q * np.array([1.1, 0.9, 1.0, 1.05]) for q in q0]
+    b = batch.Batch([(mesh, cp) for _, mesh, _, cp in cases],
+                    implicit=dict(imp, max_iter=400, restart_projected=40), **kw)
+    b.set_state(bad)
+    b.set_fallback(q0)
+    r = b.solve()
+    st, qb = b.case_status(), b.state()
+    b.close()
+    assert r["n_restarted"] == len(cases) and np.all(st["restart_iter"] == 120)
+    assert r["iterations"] == 400 and np.all(st["conv_iter"] == -1)
+    for k in range(len(cases)):
+        assert np.array_equal(qb[k], qc[k]), k
+
+
+@pytest.mark.gpu
 def test_gpu_batch_stalled_cases_retire_or_restart_once():
     """The stall test: with a 2-iteration window every case stalls within a
     few graph launches and is retired (MST_CASE_STALLED, no further cost);
