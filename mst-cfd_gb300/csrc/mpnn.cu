@@ -104,6 +104,24 @@ bool gemm_tma(const GemmArgs& a, cudaStream_t s, cudaError_t* err) {
   return true;
 }
 
+// The split-K TMA kernel where it applies (K and the chunk in tiles of 64,
+// 16-byte-aligned operands); false: the caller launches k_gemm_bf16
+bool gemm_tma_split(const GemmArgs& a, cudaStream_t s, cudaError_t* err) {
+  *err = cudaSuccess;
+  if (a.k_chunk <= 0 || a.k_chunk % kBK != 0 || a.K % kBK != 0 || a.M <= 0 || a.N <= 0 ||
+      (reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.B) & 15))
+    return false;
+  CUtensorMap ma, mb;
+  if (!bf16_tile_map(&ma, a.A, a.M, a.K) || !bf16_tile_map(&mb, a.B, a.N, a.K)) return false;
+  static std::atomic<uint64_t> attr_done{0};
+  *err = ensure_smem_limit(k_gemm_tma_split, split_smem_bytes(), attr_done);
+  if (*err != cudaSuccess) return true;
+  const dim3 grid((a.M + kBM - 1) / kBM, (a.N + kBN - 1) / kBN, (a.K + a.k_chunk - 1) / a.k_chunk);
+  k_gemm_tma_split<<<grid, kSplitThreads, split_smem_bytes(), s>>>(ma, mb, a);
+  *err = cudaGetLastError();
+  return true;
+}
+
 cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   static std::atomic<uint64_t> attr_done{0}, attr_done16{0};
   const bool narrow = a0.N <= 16;
@@ -120,7 +138,7 @@ cudaError_t gemm(const GemmArgs& a0, cudaStream_t s) {
   }();
   if (a.lbo == 0 && use_tma) {
     cudaError_t te;
-    if (gemm_tma(a, s, &te)) return te;
+    if (a.k_chunk > 0 ? gemm_tma_split(a, s, &te) : gemm_tma(a, s, &te)) return te;
   }
   if (a.lbo == 0) {
     a.lbo = kLBO;

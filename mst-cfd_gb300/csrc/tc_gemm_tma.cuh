@@ -364,5 +364,152 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
                  "r"(2 * kBN));
 }
 
+// Split-K variant for the weight gradients (M, N <= 256, K = the cells):
+// CTA (m, n, z) forms the 128x128 partial product of its K chunk and stores
+// it to C + z * M * ldc (no bias / ReLU; the caller adds the chunks in
+// order).  Warp 0 copies A and B tiles (128 x 64 each) with
+// cp.async.bulk.tensor into a ring of kSplitStages stages, warp 1 issues
+// the products into one TMEM accumulator, warps 2-5 store it.  Two CTAs per
+// SM.  The same bounded waits and drain as k_gemm_tma.
+constexpr int kSplitStages = 3;
+constexpr int kSplitThreads = 192;
+__host__ __device__ constexpr int split_smem_bytes() { return kSplitStages * 2 * kTmaTile + 256; }
+
+__global__ void __launch_bounds__(kSplitThreads)
+    k_gemm_tma_split(const __grid_constant__ CUtensorMap mapA,
+                     const __grid_constant__ CUtensorMap mapB, const GemmArgs g) {
+  constexpr int S = kSplitStages;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + S * kTmaTile;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + S * kTmaTile);
+  uint64_t* full = bars;           // [S] a stage's A and B landed
+  uint64_t* empty = bars + S;      // [S] a stage's products are done
+  uint64_t* accf = bars + 2 * S;   // the accumulator holds the chunk's product
+  uint64_t* drain = bars + 2 * S + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * S + 2);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+  const int kbase = blockIdx.z * g.k_chunk;
+  const int T = min(g.k_chunk, g.K - kbase) / kBK;
+  float* Cout = g.C + (size_t)blockIdx.z * g.M * g.ldc;
+  const unsigned lim = g.spin_limit;
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(kBN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < S; ++q) {
+      mbar_init(&full[q], 1);
+      mbar_init(&empty[q], 1);
+    }
+    mbar_init(accf, 1);
+    mbar_init(drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort = ((smem_u32(smem) & 1023) || T < 1) ? 1 : 0;
+    if (*abort) atomicExch(g.err, 2);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = !*abort;
+      uint32_t last_ph[S];
+      bool used[S];
+      for (int q = 0; q < S; ++q) used[q] = false;
+      int st = 0;
+      uint32_t ph = 0;
+      for (int k = 0; k < T && ok; ++k) {
+        if (!mbar_wait_or_abort(&empty[st], ph ^ 1, lim, abort)) {
+          ok = false;
+          break;
+        }
+        mbar_expect_tx(&full[st], (uint32_t)(2 * kTmaTile));
+        tma_load_2d(smem_u32(sA + st * kTmaTile), &mapA, kbase + k * kBK, m0, &full[st]);
+        tma_load_2d(smem_u32(sB + st * kTmaTile), &mapB, kbase + k * kBK, n0, &full[st]);
+        used[st] = true;
+        last_ph[st] = ph;
+        if (++st == S) {
+          st = 0;
+          ph ^= 1;
+        }
+      }
+      if (!ok) {
+        *abort = 1;
+        atomicCAS(g.err, 0, 1);
+      }
+      for (int q = 0; q < S; ++q)
+        if (used[q]) mbar_wait(&full[q], last_ph[q], kSpinLimit);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(kBM, kBN);
+      bool ok = !*abort, any = false;
+      int st = 0;
+      uint32_t ph = 0;
+      for (int k = 0; k < T && ok; ++k) {
+        if (!mbar_wait_or_abort(&full[st], ph, lim, abort)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(sA + st * kTmaTile), b0 = smem_u32(sB + st * kTmaTile);
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk)
+          mma_bf16(tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idesc,
+                   (k > 0 || kk > 0) ? 1u : 0u);
+        any = true;
+        mma_commit(&empty[st]);
+        if (++st == S) {
+          st = 0;
+          ph ^= 1;
+        }
+      }
+      if (ok) {
+        mma_commit(accf);
+      } else {
+        *abort = 1;
+        atomicCAS(g.err, 0, 1);
+      }
+      if (any) {
+        mma_commit(drain);
+        mbar_wait(drain, 0, kSpinLimit);
+      }
+    }
+  } else {
+    // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4).. = its rows
+    const int q = warp & 3;
+    int go = 0;
+    if (lane == 0) go = mbar_wait_or_abort(accf, 0, lim, abort) ? 1 : 0;
+    go = __shfl_sync(0xffffffffu, go, 0);
+    if (!go) {
+      if (lane == 0) {
+        *abort = 1;
+        atomicCAS(g.err, 0, 1);
+      }
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool vc = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(Cout) & 15) == 0;
+      const int row = m0 + q * 32 + lane;
+      for (int c0 = 0; c0 < kBN; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        store16(g, true, Cout, row, n0, c0, v, vc, true);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBN));
+}
+
 }  // namespace tc
 }  // namespace mst

@@ -3,9 +3,11 @@ initial field, against an FP32 numpy product of the same BF16 inputs:
 FP32 accumulation, so agreement to a few ulps of FP32 times sqrt(K).  Shapes
 with K <= 256 run the persistent TMA kernel (the large ones with several
 row tiles per CTA, both accumulators and the copy ring wrapping; 4 outputs
-in a 128-wide tile of which the copy fills the rest with zeros); K above
-256, split K and the swapped-stride layout run the cp.async kernel (its
-16-wide tile for 16 outputs or fewer)."""
+in a 128-wide tile of which the copy fills the rest with zeros); split K
+runs the split TMA kernel (one tile per CTA per chunk; 4 rows or 64
+outputs with the rest of the tile filled with zeros); K above 256 and the
+swapped-stride layout run the cp.async kernel (its 16-wide tile for 16
+outputs or fewer)."""
 import ctypes as C
 
 import numpy as np
