@@ -493,14 +493,15 @@ cudaError_t gemm(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, fl
 cudaError_t gemm_wgrad(mst_mpnn* m, const __nv_bfloat16* A, const __nv_bfloat16* B, float* C,
                        int M, int N, int K, int ldc) {
   const int kt = K / mst::tc::kBK;  // K tiles
-  // about two CTAs per SM over the output tiles, each with at least 4 K tiles
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
+  // about two CTAs per SM over the output tiles, each with at least 4 K
+  // tiles (the SM count read once, thread-safe; it only sizes the split)
+  static const int sms = [] {
+    int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      sms = 148;
-  }
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 148;
+    return n;
+  }();
   const int n_tiles = ((M + mst::tc::kBM - 1) / mst::tc::kBM) * ((N + mst::tc::kBN - 1) / mst::tc::kBN);
   const int splits =
       std::min(kMaxSplits, std::max(1, std::min(2 * sms / std::max(1, n_tiles), kt / 4)));
