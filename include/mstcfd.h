@@ -431,8 +431,8 @@ typedef struct mst_implicit_params {
   int stall_window;
   /* with fallback states set: a case not converged restart_after
    * iterations after the state was set restarts from its fallback state,
-   * once (0: off) -- e.g. a warm start held to a budget taken from the
-   * cold-start iterations of its training solves */
+   * once (0: off) -- a fixed budget; it also restarts cases that are slow
+   * but would converge, which restart_projected leaves alone */
   int restart_after;
   /* with fallback states set: every restart_projected iterations after
    * the state was set, a case whose L2, extrapolated at its rate over the
